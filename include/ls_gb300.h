@@ -1,0 +1,313 @@
+/*
+ * ls_gb300.h -- C ABI of the GB300 (sm_103a) exact-diagonalization hot path.
+ *
+ * Two groups of entry points live in libls_gb300.so:
+ *
+ *  1. Drop-in symbols.  Same names, signatures and error behaviour as the symbols that
+ *     lattice-symmetries' Haskell foreign library, its Chapel library and its Python cffi
+ *     module bind for the hot path (orbit scan, enumeration, state index, matvec).  Linking
+ *     the Haskell library against libls_gb300.so instead of kernels/libkernels.a and the
+ *     Chapel library moves basis construction and H*x onto the GPU with no source change
+ *     on the host side.  Each declaration cites the reference declaration it replaces.
+ *
+ *  2. Additive symbols (prefix ls_gpu_).  Device-pointer, stream-ordered, complex128,
+ *     multi-right-hand-side, adjoint, multi-sector and per-coupling-gradient entry points
+ *     that the reference does not have.  Nothing in group 1 depends on them.
+ *
+ * The struct layouts below restate kernels/lattice_symmetries_types.h:27-180 field by
+ * field: the Haskell host fills these structs and passes pointers across the boundary,
+ * so the byte layout must be identical.
+ */
+#pragma once
+
+#if defined(__cplusplus)
+#include <complex>
+#include <cstddef>
+#include <cstdint>
+#else
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+#endif
+
+#if defined(__cplusplus)
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------------------------------
+ * Types shared with the reference (lattice_symmetries_types.h).
+ * ------------------------------------------------------------------------------------------- */
+
+/* types.h:27-32: a Chapel-owned or foreign-owned array; `freer(elts)` releases it. */
+typedef struct {
+  void *elts;
+  uint64_t num_elts;
+  void *freer;
+} chpl_external_array;
+
+/* types.h:43-56: complex128 scalar. */
+#if defined(__cplusplus)
+typedef std::complex<double> ls_hs_scalar;
+#elif defined(LS_NO_STD_COMPLEX)
+typedef struct ls_hs_scalar {
+  double _real;
+  double _imag;
+} ls_hs_scalar;
+#else
+typedef _Complex double ls_hs_scalar;
+#endif
+
+/* The reference declares refcounts as `_Atomic int`; the representation is a plain int. */
+typedef int ls_gb300_refcount;
+
+/* types.h:81-85 */
+typedef enum ls_hs_particle_type {
+  LS_HS_SPIN,
+  LS_HS_SPINFUL_FERMION,
+  LS_HS_SPINLESS_FERMION
+} ls_hs_particle_type;
+
+/* types.h:87-98: the three basis kernel function-pointer types. */
+typedef void (*ls_hs_internal_state_index_kernel_type)(
+    ptrdiff_t batch_size, uint64_t const *alphas, ptrdiff_t alphas_stride,
+    ptrdiff_t *indices, ptrdiff_t indices_stride, void const *private_data);
+
+typedef void (*ls_hs_internal_is_representative_kernel_type)(
+    ptrdiff_t batch_size, uint64_t const *alphas, ptrdiff_t alphas_stride,
+    uint8_t *are_representatives, double *norms, void const *private_data);
+
+typedef void (*ls_hs_internal_state_info_kernel_type)(
+    ptrdiff_t batch_size, uint64_t const *alphas, ptrdiff_t alphas_stride,
+    uint64_t *betas, ptrdiff_t betas_stride, ls_hs_scalar *characters,
+    double *norms, void const *private_data);
+
+/* types.h:100-107: the basis kernel plugin table. */
+typedef struct ls_hs_basis_kernels {
+  ls_hs_internal_state_info_kernel_type state_info_kernel;
+  void *state_info_data;
+  ls_hs_internal_is_representative_kernel_type is_representative_kernel;
+  void *is_representative_data;
+  ls_hs_internal_state_index_kernel_type state_index_kernel;
+  void *state_index_data;
+} ls_hs_basis_kernels;
+
+/* types.h:109-119: a permutation group as a batched Benes network.
+ * masks: [number_shifts][number_masks] row-major, shifts: [number_shifts],
+ * eigvals_re/im: [number_masks] characters of the group elements. */
+typedef struct ls_hs_permutation_group {
+  ls_gb300_refcount refcount;
+  int number_bits;
+  int number_shifts;
+  int number_masks;
+  uint64_t *masks;
+  uint64_t *shifts;
+  double *eigvals_re;
+  double *eigvals_im;
+  void *haskell_payload;
+} ls_hs_permutation_group;
+
+/* types.h:121-133 */
+typedef struct ls_hs_basis {
+  ls_gb300_refcount refcount;
+  int number_sites;
+  int number_particles;
+  int number_up;
+  ls_hs_particle_type particle_type;
+  int spin_inversion;
+  bool state_index_is_identity;
+  bool requires_projection;
+  ls_hs_basis_kernels *kernels;
+  chpl_external_array representatives;
+  void *haskell_payload;
+} ls_hs_basis;
+
+/* types.h:140-151: non-branching terms (v, m, l, r, x, s), one 64-bit word per term. */
+typedef struct ls_hs_nonbranching_terms {
+  int number_terms;
+  int number_bits;
+  ls_hs_scalar const *v;
+  uint64_t const *m;
+  uint64_t const *l;
+  uint64_t const *r;
+  uint64_t const *x;
+  uint64_t const *s;
+} ls_hs_nonbranching_terms;
+
+/* types.h:153-161 */
+typedef struct ls_hs_operator {
+  ls_gb300_refcount refcount;
+  ls_hs_basis const *basis;
+  ls_hs_nonbranching_terms const *off_diag_terms;
+  ls_hs_nonbranching_terms const *diag_terms;
+  void *haskell_payload;
+} ls_hs_operator;
+
+/* types.h:170-180: the driver plugin table (installed by Chapel in the reference). */
+typedef struct ls_chpl_kernels {
+  void (*enumerate_states)(ls_hs_basis const *, uint64_t, uint64_t, chpl_external_array *);
+  void (*operator_apply_off_diag)(ls_hs_operator *, int64_t, uint64_t *, chpl_external_array *,
+                                  chpl_external_array *, chpl_external_array *, int64_t);
+  void (*operator_apply_diag)(ls_hs_operator *, int64_t, uint64_t *, chpl_external_array *,
+                              int64_t);
+  void (*matrix_vector_product)(ls_hs_operator *, int, double const *, double *);
+} ls_chpl_kernels;
+
+/* ---------------------------------------------------------------------------------------------
+ * 1. Drop-in symbols.
+ * ------------------------------------------------------------------------------------------- */
+
+/* Error handling: reference.c:11-36, types.h:61-74. */
+void ls_hs_set_exception_handler(void (*handler)(char const *message));
+void ls_hs_error(char const *message);
+void ls_hs_fatal_error(char const *func, int line, char const *message);
+
+/* External arrays and refcounts: reference.c:40-64, types.h:193-195. */
+void ls_hs_internal_destroy_external_array(chpl_external_array *arr);
+int ls_hs_internal_read_refcount(ls_gb300_refcount const *refcount);
+void ls_hs_internal_write_refcount(ls_gb300_refcount *refcount, int value);
+int ls_hs_internal_inc_refcount(ls_gb300_refcount *refcount);
+int ls_hs_internal_dec_refcount(ls_gb300_refcount *refcount);
+
+/* Driver plugin table: reference.c:213-225, types.h:193-194. libls_gb300.so installs its GPU
+ * drivers into the table when it is loaded and again on ls_chpl_init(). */
+ls_chpl_kernels const *ls_hs_internal_get_chpl_kernels(void);
+void ls_hs_internal_set_chpl_kernels(ls_chpl_kernels const *kernels);
+/* chapel/src/library.c:19-34 (runtime start-up / shutdown; here: install tables, create the
+ * CUDA stream / release device memory). */
+void ls_chpl_init(void);
+void ls_chpl_finalize(void);
+
+/* Orbit-scan kernel data: replaces ls_internal_create_halide_kernel_data (kernels.c:112-189,
+ * bound at Basis.hs:915-919). Uploads masks, characters and the per-site image table of the
+ * group to the GPU. spin_inversion is 0, +1 or -1. */
+void *ls_internal_create_halide_kernel_data(ls_hs_permutation_group const *group,
+                                            int spin_inversion);
+void ls_internal_destroy_halide_kernel_data(void *data);
+
+/* Orbit-scan kernels, FunPtr-compatible: replace ls_hs_is_representative_halide_kernel
+ * (kernels.c:195-244) and ls_hs_state_info_halide_kernel (kernels.c:246-319), bound at
+ * Basis.hs:921-925.  Host pointers, any strides. */
+void ls_hs_is_representative_halide_kernel(ptrdiff_t batch_size, uint64_t const *alphas,
+                                           ptrdiff_t alphas_stride, uint8_t *are_representatives,
+                                           double *norms, void const *private_data);
+void ls_hs_state_info_halide_kernel(ptrdiff_t batch_size, uint64_t const *alphas,
+                                    ptrdiff_t alphas_stride, uint64_t *betas,
+                                    ptrdiff_t betas_stride, ls_hs_scalar *characters,
+                                    double *norms, void const *private_data);
+
+/* State index: replaces indexing.c:94-125 and :273-325 (types.h:198-214; bound at
+ * Basis.hs:904-908).  The table and the search run on the GPU. */
+typedef struct ls_hs_state_index_binary_search_data ls_hs_state_index_binary_search_data;
+ls_hs_state_index_binary_search_data *ls_hs_create_state_index_binary_search_kernel_data(
+    chpl_external_array const *representatives, int number_bits, int prefix_bits);
+void ls_hs_destroy_state_index_binary_search_kernel_data(
+    ls_hs_state_index_binary_search_data *cache);
+void ls_hs_state_index_binary_search_kernel(ptrdiff_t batch_size, uint64_t const *spins,
+                                            ptrdiff_t spins_stride, ptrdiff_t *indices,
+                                            ptrdiff_t indices_stride,
+                                            void const *private_kernel_data);
+
+/* Dispatchers through basis->kernels: reference.c:137-171 (types.h:216-230). */
+void ls_hs_state_index(ls_hs_basis const *basis, ptrdiff_t batch_size, uint64_t const *spins,
+                       ptrdiff_t spins_stride, ptrdiff_t *indices, ptrdiff_t indices_stride);
+void ls_hs_is_representative(ls_hs_basis const *basis, ptrdiff_t batch_size,
+                             uint64_t const *alphas, ptrdiff_t alphas_stride,
+                             uint8_t *are_representatives, double *norms);
+void ls_hs_state_info(ls_hs_basis const *basis, ptrdiff_t batch_size, uint64_t const *alphas,
+                      ptrdiff_t alphas_stride, uint64_t *betas, ptrdiff_t betas_stride,
+                      ls_hs_scalar *characters, double *norms);
+
+/* Basis construction: reference.c:173-211 (types.h:231-235). */
+void ls_hs_build_representatives(ls_hs_basis *basis, uint64_t lower, uint64_t upper);
+void ls_hs_unchecked_set_representatives(ls_hs_basis *basis, chpl_external_array const *states,
+                                         int cache_bits);
+
+/* Combinadics: ForeignLibrary.hs:203-211 (Basis.hs:519-550). */
+ptrdiff_t ls_hs_fixed_hamming_state_to_index(uint64_t basis_state);
+uint64_t ls_hs_fixed_hamming_index_to_state(ptrdiff_t state_index, int hamming_weight);
+
+/* Term generation on the host: reference.c:67-134 (types.h:238-249). */
+void ls_internal_operator_apply_diag_x1(ls_hs_operator const *op, ptrdiff_t batch_size,
+                                        uint64_t const *alphas, double *ys, double const *xs);
+void ls_internal_operator_apply_off_diag_x1(ls_hs_operator const *op, ptrdiff_t batch_size,
+                                            uint64_t const *alphas, uint64_t *betas,
+                                            ls_hs_scalar *coeffs, ptrdiff_t *offsets,
+                                            double const *xs);
+
+/* Chapel drivers: StatesEnumeration.chpl:692-709, BatchedOperator.chpl:298-357,
+ * DistributedMatrixVector.chpl:1090-1105 (chapel/lib/lattice_symmetries_chapel.h:7-41).
+ * The matvec reads x and writes y in host memory, numVectors must be 1, exactly as in the
+ * reference; complex coefficients contribute their real part (DistributedMatrixVector.chpl:126). */
+void ls_chpl_enumerate_representatives(ls_hs_basis *p, uint64_t lower, uint64_t upper,
+                                       chpl_external_array *dest);
+void ls_chpl_operator_apply_diag(ls_hs_operator *matrix, int64_t count, uint64_t *alphas,
+                                 chpl_external_array *coeffs, int64_t num_tasks);
+void ls_chpl_operator_apply_off_diag(ls_hs_operator *matrix, int64_t count, uint64_t *alphas,
+                                     chpl_external_array *betas, chpl_external_array *coeffs,
+                                     chpl_external_array *offsets, int64_t num_tasks);
+void ls_chpl_matrix_vector_product(ls_hs_operator *matrix, int num_vectors, double const *x,
+                                   double *y);
+
+/* ---------------------------------------------------------------------------------------------
+ * 2. Additive symbols (no counterpart in the reference).
+ *
+ * All return 0 on success and a negative code on failure; ls_gpu_last_error() gives the message.
+ * `stream` is a cudaStream_t (NULL = the library's stream).  Device pointers are CUDA global
+ * memory on the current device.  Complex arrays are interleaved (re, im) float64 pairs.
+ * ------------------------------------------------------------------------------------------- */
+
+#define LS_GPU_OK 0
+#define LS_GPU_ERR_INVALID (-1)   /* bad argument */
+#define LS_GPU_ERR_CUDA (-2)      /* CUDA runtime error */
+#define LS_GPU_ERR_BASIS (-3)     /* a generated state left the basis (operator breaks a conserved number) */
+#define LS_GPU_ERR_NOT_BUILT (-4) /* basis has no representatives */
+#define LS_GPU_ERR_TIMEOUT (-5)   /* a bounded device wait gave up */
+
+char const *ls_gpu_last_error(void);
+int ls_gpu_device_synchronize(void);
+
+/* Number of representatives and device pointers of the GPU-resident basis (built by
+ * ls_hs_build_representatives or set by ls_hs_unchecked_set_representatives).  norms are the
+ * state_info norms sqrt(S/|G|) of the representatives (all 1 without projection). */
+int ls_gpu_basis_info(ls_hs_basis const *basis, int64_t *number_states,
+                      uint64_t const **d_representatives, double const **d_norms);
+
+/* y[D][k] = A x[D][k] for k right-hand sides stored row-major with leading dimension ld
+ * (ld >= k), A = H (adjoint = 0) or A = H^dagger (adjoint = 1).  Complex128 x and y.
+ * Full complex arithmetic: complex characters and coefficients are kept. */
+int ls_gpu_matvec_c128(ls_hs_operator const *op, int k, double const *d_x, int64_t ldx,
+                       double *d_y, int64_t ldy, int adjoint, void *stream);
+/* The same for real float64 vectors, with the reference's real-part semantics. */
+int ls_gpu_matvec_f64(ls_hs_operator const *op, int k, double const *d_x, int64_t ldx,
+                      double *d_y, int64_t ldy, int adjoint, void *stream);
+
+/* Per-coupling inner products out[c] = <g, H_c x> for an operator whose terms are tagged with
+ * coupling ids (term_coupling[t] in [0, n_couplings) for the off-diagonal terms, then the
+ * diagonal terms, in table order).  g, x: complex128 [D]; out: complex128 [n_couplings]
+ * (device). */
+int ls_gpu_coupling_inner_products(ls_hs_operator const *op, int n_couplings,
+                                   int32_t const *term_coupling, double const *d_g,
+                                   double const *d_x, double *d_out, void *stream);
+
+/* Multi-sector block matvec: one persistent launch over `n_sectors` operators (same term
+ * structure, different bases/characters), each with its own x/y block of k right-hand sides.
+ * Work tiles (sector, rows) are claimed from a device counter.  d_x[s], d_y[s] are device
+ * pointers with leading dimension k. */
+int ls_gpu_matvec_multi_sector_c128(int n_sectors, ls_hs_operator const *const *ops, int k,
+                                    double const *const *d_x, double *const *d_y, int adjoint,
+                                    void *stream);
+
+/* Device-side orbit scan / index on device arrays (no host staging). */
+int ls_gpu_state_info(ls_hs_basis const *basis, int64_t batch, uint64_t const *d_alphas,
+                      uint64_t *d_betas, double *d_characters, double *d_norms, void *stream);
+int ls_gpu_is_representative(ls_hs_basis const *basis, int64_t batch, uint64_t const *d_alphas,
+                             uint8_t *d_flags, double *d_norms, void *stream);
+int ls_gpu_state_index(ls_hs_basis const *basis, int64_t batch, uint64_t const *d_alphas,
+                       int64_t *d_indices, void *stream);
+
+/* Tuning knobs of the matvec kernels (rows per CTA, threads per CTA); 0 = automatic. */
+int ls_gpu_set_matvec_config(int threads_per_block, int blocks_per_sm);
+
+#if defined(__cplusplus)
+} /* extern "C" */
+#endif

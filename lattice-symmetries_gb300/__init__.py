@@ -1,0 +1,20 @@
+"""GB300-native exact-diagonalization hot path of lattice-symmetries.
+
+Import with ``importlib.import_module("lattice-symmetries_gb300")`` (the directory name is not a
+Python identifier).  The public names mirror the reference's ``lattice_symmetries`` module:
+
+    Symmetry, Symmetries, SpinBasis, SpinfulFermionBasis, SpinlessFermionBasis, Expr, Operator
+
+All numeric work (orbit scan, basis enumeration, state index, H*x) runs in libls_gb300.so on the
+GPU; importing this package fails if that library has not been built.
+"""
+
+from ._group import Symmetry, Symmetries  # noqa: F401
+from ._expr import Expr  # noqa: F401
+from . import _native  # noqa: F401
+from ._api import (Basis, Operator, SpinBasis, SpinfulFermionBasis,  # noqa: F401
+                   SpinlessFermionBasis, load_library)
+
+__version__ = "2.2.0+gb300"
+
+_native.load()

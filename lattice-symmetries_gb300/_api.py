@@ -1,0 +1,584 @@
+"""User-facing Python API mirroring the reference's python/lattice_symmetries/__init__.py.
+
+``Symmetry``, ``Symmetries``, ``SpinBasis``, ``SpinfulFermionBasis``, ``SpinlessFermionBasis``,
+``Expr`` and ``Operator`` keep the reference's names, constructor arguments and error behaviour
+(RuntimeError from the library's error handler).  Underneath, this module plays the role of the
+reference's Haskell host layer: it closes the symmetry group, writes the Benes masks and the
+non-branching term tables into the C structs of include/ls_gb300.h, and calls the C ABI of
+libls_gb300.so, whose kernels run on the GPU.
+
+Additions with no counterpart in the reference: ``Operator.matvec`` (device tensors, complex128,
+several right-hand sides, adjoint), ``Basis.device_states`` / ``device_norms``.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, byref, c_double, c_int64, c_uint8, c_uint64, c_void_p
+from typing import List, Optional, Sequence, Tuple, Union
+
+import numpy as np
+
+from . import _native as N
+from ._expr import Expr, terms_to_arrays
+from ._group import Symmetries, Symmetry
+
+try:  # scipy is optional for the LinearOperator base class
+    from scipy.sparse.linalg import LinearOperator as _LinearOperator
+except Exception:  # pragma: no cover
+    _LinearOperator = object
+
+
+def _u64(x) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(x, dtype=np.uint64))
+
+
+class _DeviceArray:
+    """Exposes a device pointer through __cuda_array_interface__ (read-only view)."""
+
+    def __init__(self, ptr: int, shape, typestr: str, owner):
+        self.__cuda_array_interface__ = {
+            "shape": tuple(shape), "typestr": typestr, "data": (int(ptr), True), "version": 3,
+            "strides": None,
+        }
+        self._owner = owner
+
+
+class Basis:
+    """Common part of the three basis kinds (reference ``Basis``, __init__.py:147-330)."""
+
+    def __init__(self, particle_type: int, number_sites: int, number_particles: int,
+                 number_up: int, spin_inversion: int, symmetries: Optional[Symmetries]):
+        lib = N.lib()
+        self._lib = lib
+        self._symmetries = symmetries if symmetries is not None else Symmetries([])
+        self._keep = []
+        self._c_kernels = N.ls_hs_basis_kernels()
+        self._c = N.ls_hs_basis()
+        c = self._c
+        c.refcount = 1
+        c.number_sites = number_sites
+        c.number_particles = number_particles
+        c.number_up = number_up
+        c.particle_type = particle_type
+        c.spin_inversion = spin_inversion
+        has_perm = particle_type == N.LS_HS_SPIN and self._symmetries.order > 0
+        c.requires_projection = bool(has_perm or spin_inversion != 0)
+        c.state_index_is_identity = self._index_is_identity()
+        c.kernels = ctypes.pointer(self._c_kernels)
+        c.representatives = N.chpl_external_array(None, 0, None)
+        self._orbit_data = None
+        if has_perm:
+            self._orbit_data = self._create_orbit_data()
+            addr_si = N.fn_address("ls_hs_state_info_halide_kernel")
+            addr_ir = N.fn_address("ls_hs_is_representative_halide_kernel")
+            self._c_kernels.state_info_kernel = addr_si
+            self._c_kernels.state_info_data = self._orbit_data
+            self._c_kernels.is_representative_kernel = addr_ir
+            self._c_kernels.is_representative_data = self._orbit_data
+
+    # -- construction helpers ---------------------------------------------------------------------
+    def _index_is_identity(self) -> bool:
+        """Basis.hs:701-707."""
+        raise NotImplementedError
+
+    def _create_orbit_data(self):
+        masks, shifts = self._symmetries.network()
+        re, im = self._symmetries.characters
+        masks = np.ascontiguousarray(masks, dtype=np.uint64)
+        shifts = np.ascontiguousarray(shifts, dtype=np.uint64)
+        g = N.ls_hs_permutation_group()
+        g.refcount = 0
+        g.number_bits = self._symmetries.number_bits
+        g.number_shifts = int(masks.shape[0])
+        g.number_masks = int(masks.shape[1]) if masks.ndim == 2 else 0
+        g.masks = N.as_ptr(masks, c_uint64)
+        g.shifts = N.as_ptr(shifts, c_uint64)
+        g.eigvals_re = N.as_ptr(re, c_double)
+        g.eigvals_im = N.as_ptr(im, c_double)
+        ptr = self._lib.ls_internal_create_halide_kernel_data(byref(g), int(self._c.spin_inversion))
+        N.check()
+        if not ptr:
+            raise RuntimeError("could not create the orbit-scan data")
+        return ptr
+
+    def __del__(self):
+        try:
+            lib = self._lib
+            k = self._c_kernels
+            if k.state_index_data:
+                lib.ls_hs_destroy_state_index_binary_search_kernel_data(k.state_index_data)
+                k.state_index_data = None
+            if self._orbit_data:
+                lib.ls_internal_destroy_halide_kernel_data(self._orbit_data)
+                self._orbit_data = None
+            if self._c.representatives.elts and self._c.representatives.freer:
+                lib.ls_hs_internal_destroy_external_array(byref(self._c.representatives))
+                self._c.representatives = N.chpl_external_array(None, 0, None)
+        except Exception:
+            pass
+
+    @property
+    def _payload(self):
+        return ctypes.pointer(self._c)
+
+    # -- reference API ----------------------------------------------------------------------------
+    @property
+    def is_built(self) -> bool:
+        return bool(self._c.representatives.elts)
+
+    def check_is_built(self):
+        if not self.is_built:
+            raise ValueError("basis states have not been built yet; "
+                             "if you wish to do so, use the basis.build() function")
+
+    @property
+    def min_state_estimate(self) -> int:
+        return self._estimates()[0]
+
+    @property
+    def max_state_estimate(self) -> int:
+        return self._estimates()[1]
+
+    def _estimates(self) -> Tuple[int, int]:
+        raise NotImplementedError
+
+    def build(self) -> None:
+        """Generate the sorted list of representatives on the GPU (ls_hs_basis_build)."""
+        if not self.is_built:
+            if self.number_bits > 64:
+                raise RuntimeError("too many bits")
+            lo, hi = self._estimates()
+            self._lib.ls_hs_build_representatives(self._payload, lo, hi)
+            N.check()
+        assert self.is_built
+
+    @property
+    def number_states(self) -> int:
+        self.check_is_built()
+        return int(self._c.representatives.num_elts)
+
+    @property
+    def states(self) -> np.ndarray:
+        n = self.number_states
+        if n == 0:
+            return np.zeros(0, dtype=np.uint64)
+        buf = (ctypes.c_uint64 * n).from_address(self._c.representatives.elts)
+        arr = np.frombuffer(buf, dtype=np.uint64)
+        arr.flags.writeable = False
+        return arr
+
+    @property
+    def number_bits(self) -> int:
+        return self._number_bits()
+
+    def _number_bits(self) -> int:
+        raise NotImplementedError
+
+    @property
+    def number_words(self) -> int:
+        return (self.number_bits + 63) // 64
+
+    @property
+    def has_spin_inversion_symmetry(self) -> bool:
+        return self._c.spin_inversion != 0
+
+    @property
+    def has_permutation_symmetries(self) -> bool:
+        return self._orbit_data is not None
+
+    @property
+    def requires_projection(self) -> bool:
+        return bool(self._c.requires_projection)
+
+    @property
+    def symmetries(self) -> Symmetries:
+        return self._symmetries
+
+    def state_info(self, x):
+        """(representatives, characters, norms), __init__.py:256-296."""
+        is_scalar = isinstance(x, (int, np.integer))
+        x = np.array([x], dtype=np.uint64) if is_scalar else _u64(x)
+        count = x.shape[0]
+        if self.has_permutation_symmetries:
+            betas = np.zeros_like(x)
+            chars = np.zeros(count, dtype=np.complex128)
+            norms = np.zeros(count, dtype=np.float64)
+            if count > 0:
+                self._lib.ls_hs_state_info(self._payload, count, N.as_ptr(x, c_uint64), 1,
+                                           N.as_ptr(betas, c_uint64), 1,
+                                           chars.ctypes.data_as(POINTER(c_double)),
+                                           N.as_ptr(norms, c_double))
+                N.check()
+        elif self.has_spin_inversion_symmetry:
+            mask = np.uint64((1 << self.number_bits) - 1)
+            b = np.bitwise_xor(x, mask)
+            when = b < x
+            betas = np.where(when, b, x)
+            chars = np.where(when, float(self._c.spin_inversion), 1.0).astype(np.complex128)
+            norms = np.ones(count, dtype=np.float64)
+        else:
+            betas = x
+            chars = np.ones(count, dtype=np.complex128)
+            norms = np.ones(count, dtype=np.float64)
+        if is_scalar:
+            return (int(betas[0]), complex(chars[0]), float(norms[0]))
+        return (betas, chars, norms)
+
+    def is_representative(self, x):
+        """(flags, raw norms) of ls_hs_is_representative."""
+        x = _u64(np.atleast_1d(x))
+        flags = np.zeros(x.shape[0], dtype=np.uint8)
+        norms = np.zeros(x.shape[0], dtype=np.float64)
+        if x.shape[0] > 0:
+            self._lib.ls_hs_is_representative(self._payload, x.shape[0], N.as_ptr(x, c_uint64), 1,
+                                              N.as_ptr(flags, c_uint8), N.as_ptr(norms, c_double))
+            N.check()
+        return flags, norms
+
+    def index(self, x):
+        """Index of basis states (-1 if absent), __init__.py:298-318."""
+        x = np.asarray(x, dtype=np.uint64, order="C")
+        is_scalar = x.ndim == 0
+        if is_scalar:
+            x = np.expand_dims(x, axis=0)
+        x = np.ascontiguousarray(x)
+        out = np.zeros(x.shape[0], dtype=np.int64)
+        if x.shape[0] > 0:
+            self.check_is_built()
+            self._lib.ls_hs_state_index(self._payload, x.shape[0], N.as_ptr(x, c_uint64), 1,
+                                        N.as_ptr(out, c_int64), 1)
+            N.check()
+        return int(out[0]) if is_scalar else out
+
+    # -- GPU views (additive) ---------------------------------------------------------------------
+    def _device_info(self):
+        self.check_is_built()
+        n = c_int64(0)
+        reps = c_void_p(0)
+        norms = c_void_p(0)
+        rc = self._lib.ls_gpu_basis_info(self._payload, byref(n), byref(reps), byref(norms))
+        N.check(rc, "ls_gpu_basis_info")
+        return n.value, reps.value, norms.value
+
+    def device_states(self):
+        """Device array of representatives (a __cuda_array_interface__ view, uint64)."""
+        n, reps, _ = self._device_info()
+        return _DeviceArray(reps, (n,), "<u8", self)
+
+    def device_norms(self):
+        n, _, norms = self._device_info()
+        return _DeviceArray(norms, (n,), "<f8", self)
+
+
+def _popcount(x: int) -> int:
+    return bin(x).count("1")
+
+
+class SpinBasis(Basis):
+    """Spin-1/2 basis (__init__.py:330-356, Basis.hs:321-345)."""
+
+    def __init__(self, number_spins: int, hamming_weight: Optional[int] = None,
+                 spin_inversion: Optional[int] = None, symmetries: Optional[Symmetries] = None):
+        n = int(number_spins)
+        if n <= 0:
+            raise ValueError("invalid number of spins: {}".format(n))
+        if hamming_weight is not None and (hamming_weight < 0 or hamming_weight > n):
+            raise ValueError("invalid Hamming weight: {}".format(hamming_weight))
+        if spin_inversion is not None and spin_inversion not in (-1, 1):
+            raise ValueError("invalid spin inversion: {}".format(spin_inversion))
+        if spin_inversion is not None and hamming_weight is None:
+            hamming_weight = n // 2
+        if spin_inversion is not None and n != 2 * hamming_weight:
+            raise ValueError("invalid spin inversion: {} spins, but Hamming weight is {}".format(
+                n, hamming_weight))
+        if symmetries is not None and symmetries.order > 0 and symmetries.number_bits != n:
+            raise ValueError("invalid symmetries")
+        self.number_spins = n
+        self.hamming_weight = hamming_weight
+        super().__init__(N.LS_HS_SPIN, n, n, -1 if hamming_weight is None else int(hamming_weight),
+                         0 if spin_inversion is None else int(spin_inversion), symmetries)
+
+    def _index_is_identity(self) -> bool:
+        return self.hamming_weight is None and self._c.spin_inversion == 0 and self._symmetries.order == 0
+
+    def _number_bits(self) -> int:
+        return self.number_spins
+
+    def _estimates(self):
+        """Basis.hs:734-774."""
+        n, h = self.number_spins, self.hamming_weight
+        if h is None:
+            return 0, (1 << n) - 1
+        lo = (1 << h) - 1
+        hi = ((1 << h) - 1) << (n - h - (1 if self._c.spin_inversion != 0 else 0))
+        return lo, hi
+
+    @property
+    def has_fixed_hamming_weight(self) -> bool:
+        return self.hamming_weight is not None
+
+    @property
+    def spin_inversion(self) -> Optional[int]:
+        i = self._c.spin_inversion
+        return int(i) if i != 0 else None
+
+
+class SpinlessFermionBasis(Basis):
+    def __init__(self, number_sites: int, number_particles: Optional[int] = None):
+        n = int(number_sites)
+        if n <= 0:
+            raise ValueError("invalid number of sites: {}".format(n))
+        if number_particles is not None and (number_particles < 0 or number_particles > n):
+            raise ValueError("invalid number of particles: {}".format(number_particles))
+        self.number_sites = n
+        self.number_particles = number_particles
+        super().__init__(N.LS_HS_SPINLESS_FERMION, n,
+                         -1 if number_particles is None else int(number_particles), -1, 0, None)
+
+    def _index_is_identity(self) -> bool:
+        return self.number_particles is None
+
+    def _number_bits(self) -> int:
+        return self.number_sites
+
+    def _estimates(self):
+        n, p = self.number_sites, self.number_particles
+        if p is None:
+            return 0, (1 << n) - 1
+        return (1 << p) - 1, ((1 << p) - 1) << (n - p)
+
+
+class SpinfulFermionBasis(Basis):
+    """Spinful fermions: bits [0, n) are the up spins, [n, 2n) the down spins (Basis.hs:621-628)."""
+
+    def __init__(self, number_sites: int, number_particles: Union[None, int, Tuple[int, int]] = None):
+        n = int(number_sites)
+        if n <= 0:
+            raise ValueError("invalid number of sites: {}".format(n))
+        self.number_sites = n
+        if number_particles is None:
+            total, up = -1, -1
+            self.occupation = None
+        elif isinstance(number_particles, (tuple, list)):
+            u, d = (int(v) for v in number_particles)
+            if u < 0 or u > n or d < 0 or d > n:
+                raise ValueError("invalid number of particles: {} up, {} down".format(u, d))
+            total, up = u + d, u
+            self.occupation = (u, d)
+        else:
+            p = int(number_particles)
+            if p < 0 or p > 2 * n:
+                raise ValueError("invalid number of particles: {}".format(p))
+            total, up = p, -1
+            self.occupation = p
+        super().__init__(N.LS_HS_SPINFUL_FERMION, n, total, up, 0, None)
+
+    def _index_is_identity(self) -> bool:
+        return self.occupation is None
+
+    def _number_bits(self) -> int:
+        return 2 * self.number_sites
+
+    def _estimates(self):
+        n = self.number_sites
+        if self.occupation is None:
+            return 0, (1 << (2 * n)) - 1
+        if isinstance(self.occupation, tuple):
+            u, d = self.occupation
+            lo = (((1 << d) - 1) << n) | ((1 << u) - 1)
+            hi = ((((1 << d) - 1) << (n - d)) << n) | (((1 << u) - 1) << (n - u))
+            return lo, hi
+        p = self.occupation
+        return (1 << p) - 1, ((1 << p) - 1) << (2 * n - p)
+
+
+def _terms_struct(arrays, number_bits: int, keep: list):
+    v, m, l, r, x, s = arrays
+    n = len(v)
+    if n == 0:
+        return None
+    v = np.ascontiguousarray(v, dtype=np.complex128)
+    arrs = [np.ascontiguousarray(a, dtype=np.uint64) for a in (m, l, r, x, s)]
+    keep.extend([v] + arrs)
+    t = N.ls_hs_nonbranching_terms()
+    t.number_terms = n
+    t.number_bits = number_bits
+    t.v = v.ctypes.data_as(POINTER(c_double))
+    t.m, t.l, t.r, t.x, t.s = (a.ctypes.data_as(POINTER(c_uint64)) for a in arrs)
+    keep.append(t)
+    return t
+
+
+class Operator(_LinearOperator):
+    """A quantum operator on a basis (__init__.py:591-759): a scipy LinearOperator on float64
+    vectors whose product runs on the GPU through ls_chpl_matrix_vector_product."""
+
+    def __init__(self, basis: Basis, expression: Expr):
+        if not isinstance(basis, Basis):
+            raise TypeError("expected a 'Basis', but got '{}'".format(type(basis)))
+        if not isinstance(expression, Expr):
+            raise TypeError("expected an 'Expr', but got '{}'".format(type(expression)))
+        self._basis = basis
+        self._expression = expression
+        n_sites = getattr(basis, "number_sites", None) or getattr(basis, "number_spins")
+        spinful = isinstance(basis, SpinfulFermionBasis)
+        terms = expression.nonbranching_terms(n_sites, spinful=spinful)
+        diag = [t for t in terms if t[4] == 0]
+        off = [t for t in terms if t[4] != 0]
+        self._diag_arrays = terms_to_arrays(diag)
+        self._off_arrays = terms_to_arrays(off)
+        self._keep = []
+        nb = basis.number_bits
+        self._c_off = _terms_struct(self._off_arrays, nb, self._keep)
+        self._c_diag = _terms_struct(self._diag_arrays, nb, self._keep)
+        self._c = N.ls_hs_operator()
+        self._c.refcount = 1
+        self._c.basis = basis._payload
+        self._c.off_diag_terms = ctypes.pointer(self._c_off) if self._c_off is not None else None
+        self._c.diag_terms = ctypes.pointer(self._c_diag) if self._c_diag is not None else None
+        self._lib = N.lib()
+
+    @property
+    def _payload(self):
+        return ctypes.pointer(self._c)
+
+    @property
+    def basis(self) -> Basis:
+        return self._basis
+
+    @property
+    def expression(self) -> Expr:
+        return self._expression
+
+    @property
+    def number_off_diag_terms(self) -> int:
+        return len(self._off_arrays[0])
+
+    @property
+    def number_diag_terms(self) -> int:
+        return len(self._diag_arrays[0])
+
+    def adjoint_operator(self) -> "Operator":
+        return Operator(self._basis, self._expression.adjoint())
+
+    def __add__(self, other):
+        return Operator(self._basis, self._expression + other._expression)
+
+    def __sub__(self, other):
+        return Operator(self._basis, self._expression - other._expression)
+
+    def scale(self, c) -> "Operator":
+        return Operator(self._basis, self._expression.scale(c))
+
+    def __rmul__(self, other):
+        if np.isscalar(other):
+            return self.scale(other)
+        return NotImplemented
+
+    def __matmul__(self, other):
+        return self.apply_to_state_vector(other)
+
+    def __repr__(self):
+        return "<Operator defined on {}>".format(self._basis.__class__.__name__)
+
+    def _check_basis_is_built(self, attribute):
+        if not self._basis.is_built:
+            raise AttributeError(
+                "'Operator' object has no attribute '{}' (did you forget to build the basis?)".format(attribute))
+
+    @property
+    def dtype(self):
+        self._check_basis_is_built("dtype")
+        return np.dtype("float64")
+
+    @property
+    def shape(self):
+        self._check_basis_is_built("shape")
+        n = self._basis.number_states
+        return (n, n)
+
+    def apply_to_state_vector(self, vector: np.ndarray) -> np.ndarray:
+        """y = H x for one float64 vector (ls_chpl_matrix_vector_product)."""
+        self._check_basis_is_built("apply_to_state_vector")
+        if vector.dtype != np.float64:
+            raise TypeError("expected a NDArray[float64], but got {}[{}]".format(
+                type(vector).__name__, type(vector.dtype)))
+        x = np.ascontiguousarray(vector)
+        out = np.empty_like(x)
+        kernels = self._lib.ls_hs_internal_get_chpl_kernels().contents
+        f = ctypes.CFUNCTYPE(None, POINTER(N.ls_hs_operator), ctypes.c_int, POINTER(c_double),
+                             POINTER(c_double))(kernels.matrix_vector_product)
+        f(self._payload, 1, N.as_ptr(x, c_double), N.as_ptr(out, c_double))
+        N.check()
+        return out
+
+    def _matvec(self, x):
+        x = np.asarray(x)
+        if x.ndim == 2:
+            return np.stack([self.apply_to_state_vector(np.ascontiguousarray(x[:, i]))
+                             for i in range(x.shape[1])], axis=1)
+        return self.apply_to_state_vector(np.ascontiguousarray(x, dtype=np.float64))
+
+    def apply_diag_to_basis_state(self, state: int) -> float:
+        arr = np.array([state], dtype=np.uint64)
+        coeffs = N.chpl_external_array()
+        self._lib.ls_chpl_operator_apply_diag(self._payload, 1, N.as_ptr(arr, c_uint64), byref(coeffs), 0)
+        N.check()
+        value = float(ctypes.cast(coeffs.elts, POINTER(c_double))[0])
+        self._lib.ls_hs_internal_destroy_external_array(byref(coeffs))
+        return value
+
+    def apply_off_diag_to_basis_state(self, state: int) -> List[Tuple[complex, int]]:
+        arr = np.array([state], dtype=np.uint64)
+        betas, coeffs, offsets = N.chpl_external_array(), N.chpl_external_array(), N.chpl_external_array()
+        self._lib.ls_chpl_operator_apply_off_diag(self._payload, 1, N.as_ptr(arr, c_uint64), byref(betas),
+                                                  byref(coeffs), byref(offsets), 0)
+        N.check()
+        count = int(ctypes.cast(offsets.elts, POINTER(ctypes.c_int64))[1])
+        out = []
+        for k in range(count):
+            c = ctypes.cast(coeffs.elts, POINTER(c_double))
+            b = ctypes.cast(betas.elts, POINTER(c_uint64))
+            out.append((complex(c[2 * k], c[2 * k + 1]), int(b[k])))
+        for a in (betas, coeffs, offsets):
+            if a.elts:
+                self._lib.ls_hs_internal_destroy_external_array(byref(a))
+        return out
+
+    # -- GPU (additive) ---------------------------------------------------------------------------
+    def matvec(self, x, out=None, adjoint: bool = False, stream=None):
+        """y = H x (or H^dagger x) on CUDA tensors: complex128 or float64, shape [D] or [D, k].
+
+        Complex arithmetic is exact (complex characters and coefficients are kept); float64
+        follows the reference's real-part semantics.
+        """
+        import torch
+
+        self._check_basis_is_built("matvec")
+        if not (isinstance(x, torch.Tensor) and x.is_cuda):
+            raise TypeError("expected a CUDA tensor")
+        if x.dtype not in (torch.complex128, torch.float64):
+            raise TypeError("expected complex128 or float64, got {}".format(x.dtype))
+        D = self._basis.number_states
+        squeeze = x.dim() == 1
+        X = x.reshape(D, 1) if squeeze else x
+        if X.dim() != 2 or X.shape[0] != D:
+            raise ValueError("expected a tensor of shape [{}] or [{}, k]".format(D, D))
+        if X.stride(1) != 1:
+            X = X.contiguous()
+        k = X.shape[1]
+        if out is None:
+            Y = torch.empty((D, k), dtype=X.dtype, device=X.device)
+        else:
+            Y = out.reshape(D, k)
+        if stream is None:
+            stream = torch.cuda.current_stream(X.device).cuda_stream
+        f = self._lib.ls_gpu_matvec_c128 if X.dtype == torch.complex128 else self._lib.ls_gpu_matvec_f64
+        rc = f(self._payload, k, X.data_ptr(), X.stride(0), Y.data_ptr(), Y.stride(0), int(adjoint), stream)
+        N.check(rc, "matvec")
+        return Y.reshape(D) if squeeze else Y
+
+
+def load_library():
+    return N.lib()

@@ -1,0 +1,1130 @@
+// abi.cu -- C ABI of libls_gb300.so: the drop-in ls_hs_* / ls_chpl_* symbols and the additive
+// ls_gpu_* symbols declared in include/ls_gb300.h.  Host logic only; kernels live in basis.cu
+// and matvec*.cu.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "lsg.h"
+
+namespace lsg {
+int set_matvec_config(int threads, int blocks_per_sm);
+}
+
+using namespace lsg;
+
+// =================================================================================================
+// Runtime state
+// =================================================================================================
+namespace {
+
+std::mutex g_mutex;  // serialises the host-pointer entry points (the reference is not re-entrant
+                     // either: reference.c:213 "not thread-safe")
+thread_local std::string g_last_error;
+
+struct Scratch {
+  void* ptr = nullptr;
+  size_t size = 0;
+};
+struct DeviceRuntime {
+  bool ready = false;
+  cudaStream_t stream = nullptr;
+  int sms = 0;
+  int* err_word = nullptr;        // device
+  uint64_t* binom = nullptr;      // device 65x65
+  Scratch dev[8];
+  Scratch host[8];
+};
+DeviceRuntime g_rt[16];
+
+int current_device() {
+  int d = 0;
+  cudaGetDevice(&d);
+  return (d >= 0 && d < 16) ? d : 0;
+}
+
+DeviceRuntime& rt() {
+  DeviceRuntime& r = g_rt[current_device()];
+  if (!r.ready) {
+    cudaStreamCreateWithFlags(&r.stream, cudaStreamNonBlocking);
+    int dev = current_device();
+    cudaDeviceGetAttribute(&r.sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaMalloc((void**)&r.err_word, 4 * sizeof(int));
+    cudaMemset(r.err_word, 0, 4 * sizeof(int));
+    uint64_t table[65][65];
+    memset(table, 0, sizeof(table));
+    table[0][0] = 1;
+    for (int n = 1; n <= 64; ++n) {
+      table[n][0] = 1;
+      for (int k = 1; k <= n; ++k) table[n][k] = table[n - 1][k - 1] + table[n - 1][k];
+    }
+    cudaMalloc((void**)&r.binom, sizeof(table));
+    cudaMemcpy(r.binom, table, sizeof(table), cudaMemcpyHostToDevice);
+    r.ready = true;
+  }
+  return r;
+}
+
+// default handler: print and abort, like reference.c:20-23
+void default_error_handler(char const* message) {
+  fprintf(stderr, "[Error]   %s\n[Error]   Aborting ...", message);
+  abort();
+}
+std::atomic<void (*)(char const*)> g_handler{&default_error_handler};
+
+}  // namespace
+
+namespace lsg {
+
+cudaStream_t default_stream() { return rt().stream; }
+int num_sms() { return std::max(1, rt().sms); }
+void set_error(const std::string& msg) { g_last_error = msg; }
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+bool cuda_ok(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return true;
+  g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return false;
+}
+int* device_error_word() { return rt().err_word; }
+const uint64_t* device_binomials() { return rt().binom; }
+
+void* scratch(size_t bytes, int slot) {
+  Scratch& s = rt().dev[slot];
+  if (s.size < bytes) {
+    if (s.ptr) cudaFree(s.ptr);
+    s.ptr = nullptr;
+    s.size = 0;
+    size_t want = std::max<size_t>(bytes, 1 << 20);
+    if (cudaMalloc(&s.ptr, want) != cudaSuccess) {
+      s.ptr = nullptr;
+      g_last_error = "out of device memory for a scratch buffer";
+      return nullptr;
+    }
+    s.size = want;
+  }
+  return s.ptr;
+}
+
+void* pinned_scratch(size_t bytes, int slot) {
+  Scratch& s = rt().host[slot];
+  if (s.size < bytes) {
+    if (s.ptr) cudaFreeHost(s.ptr);
+    s.ptr = nullptr;
+    s.size = 0;
+    size_t want = std::max<size_t>(bytes, 1 << 20);
+    if (cudaMallocHost(&s.ptr, want) != cudaSuccess) {
+      s.ptr = nullptr;
+      g_last_error = "out of pinned host memory for a staging buffer";
+      return nullptr;
+    }
+    s.size = want;
+  }
+  return s.ptr;
+}
+
+}  // namespace lsg
+
+// =================================================================================================
+// Error handling (reference.c:11-36)
+// =================================================================================================
+extern "C" void ls_hs_fatal_error(char const* func, int line, char const* message) {
+  fprintf(stderr, "[Error]   [%s#%i] %s\n[Error]   Aborting ...", func, line, message);
+  abort();
+}
+
+extern "C" void ls_hs_set_exception_handler(void (*handler)(char const* message)) {
+  g_handler.store(handler == nullptr ? &default_error_handler : handler);
+}
+
+extern "C" void ls_hs_error(char const* message) {
+  auto h = g_handler.load();
+  if (h == nullptr) ls_hs_fatal_error(__func__, __LINE__, "error handler is NULL");
+  h(message);
+}
+
+static void report(const char* prefix) {
+  std::string m = std::string(prefix) + (g_last_error.empty() ? "" : (": " + g_last_error));
+  ls_hs_error(m.c_str());
+}
+
+extern "C" char const* ls_gpu_last_error(void) { return g_last_error.c_str(); }
+
+// =================================================================================================
+// External arrays and refcounts (reference.c:38-64)
+// =================================================================================================
+extern "C" void ls_hs_internal_destroy_external_array(chpl_external_array* arr) {
+  if (arr == nullptr) ls_hs_fatal_error(__func__, __LINE__, "trying to destroy a NULL chpl_external_array");
+  if (arr->freer != nullptr) {
+    auto f = (void (*)(void*))arr->freer;
+    f(arr->elts);
+  }
+}
+extern "C" int ls_hs_internal_read_refcount(ls_gb300_refcount const* rc) {
+  return __atomic_load_n(rc, __ATOMIC_SEQ_CST);
+}
+extern "C" void ls_hs_internal_write_refcount(ls_gb300_refcount* rc, int value) {
+  __atomic_store_n(rc, value, __ATOMIC_SEQ_CST);
+}
+extern "C" int ls_hs_internal_inc_refcount(ls_gb300_refcount* rc) {
+  return __atomic_fetch_add(rc, 1, __ATOMIC_SEQ_CST);
+}
+extern "C" int ls_hs_internal_dec_refcount(ls_gb300_refcount* rc) {
+  return __atomic_fetch_sub(rc, 1, __ATOMIC_SEQ_CST);
+}
+
+static void free_pinned(void* p) {
+  if (p) cudaFreeHost(p);
+}
+static void free_malloced(void* p) { free(p); }
+
+// =================================================================================================
+// Plugin table (reference.c:213-225) and library start-up
+// =================================================================================================
+static ls_chpl_kernels g_chpl_kernels = {nullptr, nullptr, nullptr, nullptr};
+
+extern "C" ls_chpl_kernels const* ls_hs_internal_get_chpl_kernels(void) { return &g_chpl_kernels; }
+extern "C" void ls_hs_internal_set_chpl_kernels(ls_chpl_kernels const* kernels) {
+  g_chpl_kernels = *kernels;
+}
+
+static void install_gpu_drivers() {
+  ls_chpl_kernels k;
+  k.enumerate_states = (void (*)(ls_hs_basis const*, uint64_t, uint64_t, chpl_external_array*))
+      & ls_chpl_enumerate_representatives;
+  k.operator_apply_off_diag = &ls_chpl_operator_apply_off_diag;
+  k.operator_apply_diag = &ls_chpl_operator_apply_diag;
+  k.matrix_vector_product = &ls_chpl_matrix_vector_product;
+  ls_hs_internal_set_chpl_kernels(&k);
+}
+
+// The reference's Chapel library installs its drivers when its module initialises
+// (LatticeSymmetries.chpl:17-32); this library does the same when it is loaded.
+__attribute__((constructor)) static void lsg_on_load() { install_gpu_drivers(); }
+
+extern "C" void ls_chpl_init(void) { install_gpu_drivers(); }
+extern "C" void ls_chpl_finalize(void) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  for (int d = 0; d < 16; ++d) {
+    DeviceRuntime& r = g_rt[d];
+    if (!r.ready) continue;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(d);
+    for (auto& s : r.dev) {
+      if (s.ptr) cudaFree(s.ptr);
+      s = Scratch{};
+    }
+    for (auto& s : r.host) {
+      if (s.ptr) cudaFreeHost(s.ptr);
+      s = Scratch{};
+    }
+    cudaSetDevice(prev);
+  }
+}
+
+extern "C" int ls_gpu_device_synchronize(void) {
+  return cuda_ok(cudaStreamSynchronize(default_stream()), "synchronize") ? 0 : LS_GPU_ERR_CUDA;
+}
+
+extern "C" int ls_gpu_set_matvec_config(int threads_per_block, int blocks_per_sm) {
+  if (threads_per_block != 0 && (threads_per_block % 32 != 0 || threads_per_block > 1024))
+    return fail(LS_GPU_ERR_INVALID, "threads_per_block must be a multiple of 32, at most 1024");
+  return set_matvec_config(threads_per_block, blocks_per_sm);
+}
+
+// =================================================================================================
+// Orbit-scan kernel data (kernels.c:112-193)
+// =================================================================================================
+extern "C" void* ls_internal_create_halide_kernel_data(ls_hs_permutation_group const* g,
+                                                       int spin_inversion) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (g == nullptr) {
+    set_error("permutation group is NULL");
+    report("ls_internal_create_halide_kernel_data");
+    return nullptr;
+  }
+  if (spin_inversion != 0 && spin_inversion != 1 && spin_inversion != -1)
+    ls_hs_fatal_error(__func__, __LINE__, "invalid spin_inversion");
+  if (g->number_bits < 0 || g->number_bits > 64 || g->number_masks < 0 ||
+      g->number_masks > kMaxGroupElements || g->number_shifts < 0 || g->number_shifts > 64) {
+    set_error("unsupported permutation group (bits <= 64, |G| <= 2048)");
+    report("ls_internal_create_halide_kernel_data");
+    return nullptr;
+  }
+  OrbitData* od = new OrbitData();
+  od->magic = kOrbitMagic;
+  od->n_bits = g->number_bits;
+  od->n_elems = g->number_masks;
+  od->depth = g->number_shifts;
+  od->spin_inversion = spin_inversion;
+  const size_t nm = (size_t)od->depth * od->n_elems;
+  od->masks.assign(g->masks, g->masks + nm);
+  od->shifts.resize(od->depth);
+  for (int k = 0; k < od->depth; ++k) od->shifts[k] = (uint32_t)g->shifts[k];
+  od->chars_re.assign(g->eigvals_re, g->eigvals_re + od->n_elems);
+  od->chars_im.assign(g->eigvals_im, g->eigvals_im + od->n_elems);
+  if (compute_site_images(od) != 0) {
+    report("ls_internal_create_halide_kernel_data");
+    delete od;
+    return nullptr;
+  }
+  return od;
+}
+
+extern "C" void ls_internal_destroy_halide_kernel_data(void* p) {
+  if (p == nullptr) return;
+  OrbitData* od = (OrbitData*)p;
+  if (od->magic != kOrbitMagic) return;
+  if (od->dev_block) cudaFree(od->dev_block);
+  od->magic = 0;
+  delete od;
+}
+
+// Host-pointer staging helpers ------------------------------------------------------------------
+static const uint64_t* stage_alphas(ptrdiff_t n, uint64_t const* alphas, ptrdiff_t stride, int slot) {
+  uint64_t* h = (uint64_t*)pinned_scratch((size_t)n * 8, slot);
+  uint64_t* d = (uint64_t*)scratch((size_t)n * 8, slot);
+  if (!h || !d) return nullptr;
+  if (stride == 1) {
+    memcpy(h, alphas, (size_t)n * 8);
+  } else {
+    for (ptrdiff_t i = 0; i < n; ++i) h[i] = alphas[i * stride];
+  }
+  if (!cuda_ok(cudaMemcpyAsync(d, h, (size_t)n * 8, cudaMemcpyHostToDevice, default_stream()), "H2D"))
+    return nullptr;
+  return d;
+}
+
+extern "C" void ls_hs_state_info_halide_kernel(ptrdiff_t batch_size, uint64_t const* alphas,
+                                               ptrdiff_t alphas_stride, uint64_t* betas,
+                                               ptrdiff_t betas_stride, ls_hs_scalar* characters,
+                                               double* norms, void const* private_data) {
+  if (batch_size <= 0) return;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  const OrbitData* od = (const OrbitData*)private_data;
+  if (od == nullptr || od->magic != kOrbitMagic) {
+    set_error("invalid kernel data");
+    report("ls_hs_state_info");
+    return;
+  }
+  cudaStream_t s = default_stream();
+  const uint64_t* d_x = stage_alphas(batch_size, alphas, alphas_stride, 0);
+  uint64_t* d_r = (uint64_t*)scratch((size_t)batch_size * 8, 1);
+  double2* d_c = (double2*)scratch((size_t)batch_size * 16, 2);
+  double* d_n = (double*)scratch((size_t)batch_size * 8, 3);
+  uint8_t* h = (uint8_t*)pinned_scratch((size_t)batch_size * 32, 1);
+  if (!d_x || !d_r || !d_c || !d_n || !h) {
+    report("ls_hs_state_info");
+    return;
+  }
+  const DeviceGroup* dg = od->n_elems > 0 ? orbit_device(od) : nullptr;
+  int rc = dg ? launch_state_info(*dg, batch_size, d_x, d_r, d_c, d_n, 8, s) : LS_GPU_ERR_CUDA;
+  if (od->n_elems == 0) {
+    set_error("state_info requires a non-empty symmetry group");
+    rc = LS_GPU_ERR_INVALID;
+  }
+  uint64_t* hr = (uint64_t*)h;
+  double2* hc = (double2*)(h + (size_t)batch_size * 8);
+  double* hn = (double*)(h + (size_t)batch_size * 24);
+  if (rc == 0 &&
+      (!cuda_ok(cudaMemcpyAsync(hr, d_r, (size_t)batch_size * 8, cudaMemcpyDeviceToHost, s), "D2H") ||
+       !cuda_ok(cudaMemcpyAsync(hc, d_c, (size_t)batch_size * 16, cudaMemcpyDeviceToHost, s), "D2H") ||
+       !cuda_ok(cudaMemcpyAsync(hn, d_n, (size_t)batch_size * 8, cudaMemcpyDeviceToHost, s), "D2H") ||
+       !cuda_ok(cudaStreamSynchronize(s), "state_info")))
+    rc = LS_GPU_ERR_CUDA;
+  if (rc != 0) {
+    report("ls_hs_state_info");
+    return;
+  }
+  double* cout = reinterpret_cast<double*>(characters);
+  for (ptrdiff_t i = 0; i < batch_size; ++i) {
+    betas[i * betas_stride] = hr[i];
+    cout[2 * i] = hc[i].x;
+    cout[2 * i + 1] = hc[i].y;
+    norms[i] = hn[i];
+  }
+}
+
+extern "C" void ls_hs_is_representative_halide_kernel(ptrdiff_t batch_size, uint64_t const* alphas,
+                                                      ptrdiff_t alphas_stride,
+                                                      uint8_t* are_representatives, double* norms,
+                                                      void const* private_data) {
+  if (batch_size <= 0) return;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  const OrbitData* od = (const OrbitData*)private_data;
+  if (od == nullptr || od->magic != kOrbitMagic || od->n_elems == 0) {
+    set_error("invalid kernel data or empty group");
+    report("ls_hs_is_representative");
+    return;
+  }
+  cudaStream_t s = default_stream();
+  const uint64_t* d_x = stage_alphas(batch_size, alphas, alphas_stride, 0);
+  uint8_t* d_f = (uint8_t*)scratch((size_t)batch_size, 1);
+  double* d_n = (double*)scratch((size_t)batch_size * 8, 2);
+  uint8_t* h = (uint8_t*)pinned_scratch((size_t)batch_size * 16, 1);
+  if (!d_x || !d_f || !d_n || !h) {
+    report("ls_hs_is_representative");
+    return;
+  }
+  const DeviceGroup* dg = orbit_device(od);
+  int rc = dg ? launch_is_representative(*dg, batch_size, d_x, d_f, d_n, 4, s) : LS_GPU_ERR_CUDA;
+  double* hn = (double*)h;
+  uint8_t* hf = h + (size_t)batch_size * 8;
+  if (rc == 0 &&
+      (!cuda_ok(cudaMemcpyAsync(hn, d_n, (size_t)batch_size * 8, cudaMemcpyDeviceToHost, s), "D2H") ||
+       !cuda_ok(cudaMemcpyAsync(hf, d_f, (size_t)batch_size, cudaMemcpyDeviceToHost, s), "D2H") ||
+       !cuda_ok(cudaStreamSynchronize(s), "is_representative")))
+    rc = LS_GPU_ERR_CUDA;
+  if (rc != 0) {
+    report("ls_hs_is_representative");
+    return;
+  }
+  memcpy(are_representatives, hf, (size_t)batch_size);
+  memcpy(norms, hn, (size_t)batch_size * 8);
+}
+
+// =================================================================================================
+// State index (indexing.c:94-125, :273-325)
+// =================================================================================================
+namespace {
+// Device copies of representatives produced by the GPU enumeration, keyed by the host array they
+// were copied to, so that building the index does not upload them again.
+std::unordered_map<const void*, uint64_t*> g_pending_device_reps;
+}
+
+struct ls_hs_state_index_binary_search_data : IndexData {};
+
+extern "C" ls_hs_state_index_binary_search_data* ls_hs_create_state_index_binary_search_kernel_data(
+    chpl_external_array const* representatives, int number_bits, int prefix_bits) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (representatives == nullptr) ls_hs_fatal_error(__func__, __LINE__, "representatives is NULL");
+  if (!(0 < number_bits && number_bits <= 64))
+    ls_hs_fatal_error(__func__, __LINE__, "invalid bits");
+  auto* ix = new ls_hs_state_index_binary_search_data();
+  ix->magic = kIndexMagic;
+  ix->n_states = (int64_t)representatives->num_elts;
+  ix->host_reps = (const uint64_t*)representatives->elts;
+  ix->number_bits = number_bits;
+  ix->prefix_bits = std::min(prefix_bits, number_bits);
+  cudaStream_t s = default_stream();
+  auto it = g_pending_device_reps.find(representatives->elts);
+  if (it != g_pending_device_reps.end()) {
+    ix->d_reps = it->second;
+    g_pending_device_reps.erase(it);
+  } else {
+    if (!cuda_ok(cudaMalloc((void**)&ix->d_reps, std::max<int64_t>(ix->n_states, 1) * 8), "cudaMalloc(reps)") ||
+        (ix->n_states > 0 &&
+         !cuda_ok(cudaMemcpyAsync(ix->d_reps, ix->host_reps, (size_t)ix->n_states * 8,
+                                  cudaMemcpyHostToDevice, s), "upload reps"))) {
+      report("ls_hs_create_state_index_binary_search_kernel_data");
+      delete ix;
+      return nullptr;
+    }
+  }
+  int shift = 0;
+  int64_t range = 0;
+  if (build_prefix_index(ix->d_reps, ix->n_states, number_bits, ix->prefix_bits, &ix->d_offsets,
+                         &range, &shift, s) != 0 ||
+      !cuda_ok(cudaStreamSynchronize(s), "build index")) {
+    report("ls_hs_create_state_index_binary_search_kernel_data");
+    cudaFree(ix->d_reps);
+    delete ix;
+    return nullptr;
+  }
+  ix->dev.n_states = ix->n_states;
+  ix->dev.reps = ix->d_reps;
+  ix->dev.offsets = ix->d_offsets;
+  ix->dev.shift = shift;
+  ix->dev.range_size = range;
+  ix->dev.prefix_bits = ix->prefix_bits;
+  return ix;
+}
+
+extern "C" void ls_hs_destroy_state_index_binary_search_kernel_data(
+    ls_hs_state_index_binary_search_data* cache) {
+  if (cache == nullptr || cache->magic != kIndexMagic) return;
+  cudaFree(cache->d_reps);
+  cudaFree(cache->d_offsets);
+  cudaFree(cache->d_norms);
+  cache->magic = 0;
+  delete cache;
+}
+
+extern "C" void ls_hs_state_index_binary_search_kernel(ptrdiff_t batch_size, uint64_t const* spins,
+                                                       ptrdiff_t spins_stride, ptrdiff_t* indices,
+                                                       ptrdiff_t indices_stride,
+                                                       void const* private_kernel_data) {
+  if (indices_stride != 1) ls_hs_fatal_error(__func__, __LINE__, "expected indices_stride==1");
+  if (spins_stride != 1) ls_hs_fatal_error(__func__, __LINE__, "expected spins_stride==1");
+  if (batch_size <= 0) return;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  const IndexData* ix = (const IndexData*)private_kernel_data;
+  if (ix == nullptr || ix->magic != kIndexMagic) {
+    set_error("invalid index data");
+    report("ls_hs_state_index");
+    return;
+  }
+  cudaStream_t s = default_stream();
+  const uint64_t* d_x = stage_alphas(batch_size, spins, 1, 0);
+  int64_t* d_i = (int64_t*)scratch((size_t)batch_size * 8, 1);
+  if (!d_x || !d_i) {
+    report("ls_hs_state_index");
+    return;
+  }
+  int rc = launch_state_index(ix->dev, batch_size, d_x, d_i, s);
+  if (rc == 0 && (!cuda_ok(cudaMemcpyAsync(indices, d_i, (size_t)batch_size * 8, cudaMemcpyDeviceToHost, s), "D2H") ||
+                  !cuda_ok(cudaStreamSynchronize(s), "state_index")))
+    rc = LS_GPU_ERR_CUDA;
+  if (rc != 0) report("ls_hs_state_index");
+}
+
+// =================================================================================================
+// Dispatchers (reference.c:137-171)
+// =================================================================================================
+extern "C" void ls_hs_state_index(ls_hs_basis const* basis, ptrdiff_t batch_size, uint64_t const* spins,
+                                  ptrdiff_t spins_stride, ptrdiff_t* indices, ptrdiff_t indices_stride) {
+  if (basis->kernels->state_index_kernel == nullptr)
+    ls_hs_fatal_error(__func__, __LINE__, "state_index_kernel is NULL");
+  basis->kernels->state_index_kernel(batch_size, spins, spins_stride, indices, indices_stride,
+                                     basis->kernels->state_index_data);
+}
+
+extern "C" void ls_hs_is_representative(ls_hs_basis const* basis, ptrdiff_t batch_size,
+                                        uint64_t const* alphas, ptrdiff_t alphas_stride,
+                                        uint8_t* are_representatives, double* norms) {
+  if (basis->kernels->is_representative_kernel == nullptr)
+    ls_hs_fatal_error(__func__, __LINE__,
+                      "is_representative_kernel is NULL, perhaps this basis requires no projection?");
+  basis->kernels->is_representative_kernel(batch_size, alphas, alphas_stride, are_representatives,
+                                           norms, basis->kernels->is_representative_data);
+}
+
+extern "C" void ls_hs_state_info(ls_hs_basis const* basis, ptrdiff_t batch_size, uint64_t const* alphas,
+                                 ptrdiff_t alphas_stride, uint64_t* betas, ptrdiff_t betas_stride,
+                                 ls_hs_scalar* characters, double* norms) {
+  if (basis->kernels->state_info_kernel == nullptr)
+    ls_hs_fatal_error(__func__, __LINE__,
+                      "state_info_kernel is NULL, perhaps this basis requires no projection?");
+  basis->kernels->state_info_kernel(batch_size, alphas, alphas_stride, betas, betas_stride,
+                                    characters, norms, basis->kernels->state_info_data);
+}
+
+// =================================================================================================
+// Basis helpers
+// =================================================================================================
+static int basis_number_bits(ls_hs_basis const* b) {
+  return (b->particle_type == LS_HS_SPINFUL_FERMION ? 2 : 1) * b->number_sites;
+}
+
+static const OrbitData* basis_orbit(ls_hs_basis const* b) {
+  if (b->kernels == nullptr) return nullptr;
+  if (b->kernels->state_info_kernel != &ls_hs_state_info_halide_kernel) return nullptr;
+  const OrbitData* od = (const OrbitData*)b->kernels->state_info_data;
+  return (od && od->magic == kOrbitMagic) ? od : nullptr;
+}
+
+static IndexData* basis_index(ls_hs_basis const* b) {
+  if (b->kernels == nullptr) return nullptr;
+  if (b->kernels->state_index_kernel != &ls_hs_state_index_binary_search_kernel) return nullptr;
+  IndexData* ix = (IndexData*)b->kernels->state_index_data;
+  return (ix && ix->magic == kIndexMagic) ? ix : nullptr;
+}
+
+static bool has_permutations(ls_hs_basis const* b) {
+  const OrbitData* od = basis_orbit(b);
+  return b->particle_type == LS_HS_SPIN && od != nullptr && od->n_elems > 0;
+}
+
+static bool hamming_fixed(ls_hs_basis const* b) {
+  if (b->particle_type == LS_HS_SPIN) return b->number_up >= 0;
+  return b->number_particles >= 0;
+}
+
+static uint64_t low_ones(int k) { return k <= 0 ? 0 : (k >= 64 ? ~0ull : ((1ull << k) - 1)); }
+
+// Basis.hs:734-774 for a spin / spinless-like description.
+static void estimate_fixed(int n, int h, bool inversion, uint64_t* lo, uint64_t* hi) {
+  if (h < 0) {
+    *lo = 0;
+    *hi = low_ones(n);
+    return;
+  }
+  *lo = low_ones(h);
+  const int sh = inversion ? n - h - 1 : n - h;
+  *hi = (sh >= 64 || sh < 0) ? 0 : (low_ones(h) << sh);
+}
+
+static void state_estimates(ls_hs_basis const* b, uint64_t* lo, uint64_t* hi) {
+  const int n = b->number_sites;
+  if (b->particle_type == LS_HS_SPIN) {
+    estimate_fixed(n, b->number_up, b->spin_inversion != 0, lo, hi);
+  } else if (b->particle_type == LS_HS_SPINLESS_FERMION) {
+    estimate_fixed(n, b->number_particles, false, lo, hi);
+  } else {
+    if (b->number_up >= 0) {
+      uint64_t l0, h0, l1, h1;
+      estimate_fixed(n, b->number_up, false, &l0, &h0);
+      estimate_fixed(n, b->number_particles - b->number_up, false, &l1, &h1);
+      *lo = (l1 << n) | l0;
+      *hi = (h1 << n) | h0;
+    } else {
+      estimate_fixed(2 * n, b->number_particles, false, lo, hi);
+    }
+  }
+}
+
+static DeviceConstraint basis_constraint(ls_hs_basis const* b) {
+  DeviceConstraint c;
+  if (b->particle_type == LS_HS_SPIN) {
+    if (b->number_up >= 0) {
+      c.kind = 1;
+      c.w0 = b->number_up;
+    }
+  } else if (b->particle_type == LS_HS_SPINLESS_FERMION) {
+    if (b->number_particles >= 0) {
+      c.kind = 1;
+      c.w0 = b->number_particles;
+    }
+  } else {
+    if (b->number_up >= 0) {
+      c.kind = 2;
+      c.half_bits = b->number_sites;
+      c.w0 = b->number_up;
+      c.w1 = b->number_particles - b->number_up;
+    } else if (b->number_particles >= 0) {
+      c.kind = 1;
+      c.w0 = b->number_particles;
+    }
+  }
+  return c;
+}
+
+// =================================================================================================
+// Enumeration driver (StatesEnumeration.chpl:674-709)
+// =================================================================================================
+static int enumerate_into(ls_hs_basis const* b, uint64_t** d_out, int64_t* count) {
+  EnumerateRequest req{};
+  uint64_t lo, hi;
+  state_estimates(b, &lo, &hi);
+  req.lower = lo;
+  req.upper = hi;
+  req.number_sites = b->number_sites;
+  req.spin_inversion = b->spin_inversion;
+  req.hamming_fixed = hamming_fixed(b);
+  req.reference_norm_rule = 1;
+  const OrbitData* od = basis_orbit(b);
+  const DeviceGroup* g = nullptr;
+  if (b->particle_type == LS_HS_SPIN) {
+    if (has_permutations(b)) {
+      req.mode = 0;
+      g = orbit_device(od);
+      if (g == nullptr) return LS_GPU_ERR_CUDA;
+    } else {
+      req.mode = 1;
+    }
+  } else if (b->particle_type == LS_HS_SPINFUL_FERMION) {
+    req.mode = b->number_up >= 0 ? 2 : 1;
+    req.spin_inversion = 0;
+  } else {
+    req.mode = 1;
+    req.spin_inversion = 0;
+  }
+  if (req.mode == 1 && b->particle_type == LS_HS_SPINFUL_FERMION) req.number_sites = 2 * b->number_sites;
+  return enumerate_states(g, req, d_out, count, default_stream());
+}
+
+extern "C" void ls_chpl_enumerate_representatives(ls_hs_basis* p, uint64_t lower, uint64_t upper,
+                                                  chpl_external_array* dest) {
+  (void)lower;  // the reference derives the range from the basis (StatesEnumeration.chpl:683-689)
+  (void)upper;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (basis_number_bits(p) > 64) {
+    set_error("bases with more than 64 bits are not yet implemented");
+    report("ls_chpl_enumerate_representatives");
+    return;
+  }
+  uint64_t* d = nullptr;
+  int64_t n = 0;
+  cudaStream_t s = default_stream();
+  if (enumerate_into(p, &d, &n) != 0) {
+    report("ls_chpl_enumerate_representatives");
+    return;
+  }
+  uint64_t* h = nullptr;
+  if (!cuda_ok(cudaMallocHost((void**)&h, std::max<int64_t>(n, 1) * 8), "cudaMallocHost(reps)") ||
+      (n > 0 && !cuda_ok(cudaMemcpyAsync(h, d, (size_t)n * 8, cudaMemcpyDeviceToHost, s), "D2H reps")) ||
+      !cuda_ok(cudaStreamSynchronize(s), "enumerate")) {
+    cudaFree(d);
+    report("ls_chpl_enumerate_representatives");
+    return;
+  }
+  g_pending_device_reps[h] = d;
+  dest->elts = h;
+  dest->num_elts = (uint64_t)n;
+  dest->freer = (void*)&free_pinned;
+}
+
+// reference.c:173-194
+extern "C" void ls_hs_build_representatives(ls_hs_basis* basis, uint64_t lower, uint64_t upper) {
+  ls_chpl_kernels const* kernels = ls_hs_internal_get_chpl_kernels();
+  if (kernels->enumerate_states == nullptr)
+    ls_hs_fatal_error(__func__, __LINE__, "enumerate_states kernel is NULL");
+  if (basis->representatives.num_elts > 0) return;
+  chpl_external_array arr{nullptr, 0, nullptr};
+  kernels->enumerate_states(basis, lower, upper, &arr);
+  if (arr.elts == nullptr && arr.num_elts == 0 && !g_last_error.empty()) {
+    // error already reported through ls_hs_error
+  }
+  basis->representatives = arr;
+  const int number_bits = basis_number_bits(basis);
+  basis->kernels->state_index_data =
+      ls_hs_create_state_index_binary_search_kernel_data(&basis->representatives, number_bits, 22);
+  basis->kernels->state_index_kernel = &ls_hs_state_index_binary_search_kernel;
+}
+
+// reference.c:196-211
+extern "C" void ls_hs_unchecked_set_representatives(ls_hs_basis* basis, chpl_external_array const* states,
+                                                    int cache_bits) {
+  if (basis->representatives.num_elts != 0)
+    ls_hs_fatal_error(__func__, __LINE__, "representatives have already been set");
+  if (basis->kernels == nullptr) ls_hs_fatal_error(__func__, __LINE__, "basis->kernels not set");
+  if (basis->kernels->state_index_kernel != nullptr)
+    ls_hs_fatal_error(__func__, __LINE__, "state_index_kernel has already been set");
+  basis->representatives = *states;
+  basis->kernels->state_index_data = ls_hs_create_state_index_binary_search_kernel_data(
+      &basis->representatives, basis_number_bits(basis), cache_bits);
+  basis->kernels->state_index_kernel = &ls_hs_state_index_binary_search_kernel;
+}
+
+extern "C" ptrdiff_t ls_hs_fixed_hamming_state_to_index(uint64_t basis_state) {
+  return (ptrdiff_t)fixed_hamming_state_to_index(basis_state);
+}
+extern "C" uint64_t ls_hs_fixed_hamming_index_to_state(ptrdiff_t state_index, int hamming_weight) {
+  return fixed_hamming_index_to_state((int64_t)state_index, hamming_weight);
+}
+
+// =================================================================================================
+// Host term generation (reference.c:67-134 semantics)
+// =================================================================================================
+static inline double creal_of(ls_hs_scalar const& v) { return reinterpret_cast<const double*>(&v)[0]; }
+static inline double cimag_of(ls_hs_scalar const& v) { return reinterpret_cast<const double*>(&v)[1]; }
+
+extern "C" void ls_internal_operator_apply_diag_x1(ls_hs_operator const* op, ptrdiff_t batch_size,
+                                                   uint64_t const* alphas, double* ys, double const* xs) {
+  if (op->diag_terms == nullptr || op->diag_terms->number_terms == 0) {
+    memset(ys, 0, (size_t)batch_size * sizeof(double));
+    return;
+  }
+  ls_hs_nonbranching_terms const* t = op->diag_terms;
+  for (ptrdiff_t i = 0; i < batch_size; ++i) {
+    double acc = 0;
+    const uint64_t a = alphas[i];
+    for (int k = 0; k < t->number_terms; ++k) {
+      if ((a & t->m[k]) == t->r[k]) {
+        const int sign = 1 - 2 * (__builtin_popcountll(a & t->s[k]) % 2);
+        const double factor = xs != nullptr ? sign * xs[i] : (double)sign;
+        acc += creal_of(t->v[k]) * factor;
+      }
+    }
+    ys[i] = acc;
+  }
+}
+
+extern "C" void ls_internal_operator_apply_off_diag_x1(ls_hs_operator const* op, ptrdiff_t batch_size,
+                                                       uint64_t const* alphas, uint64_t* betas,
+                                                       ls_hs_scalar* coeffs, ptrdiff_t* offsets,
+                                                       double const* xs) {
+  if (op->off_diag_terms == nullptr || op->off_diag_terms->number_terms == 0) {
+    memset(offsets, 0, (size_t)(batch_size + 1) * sizeof(ptrdiff_t));
+    return;
+  }
+  ls_hs_nonbranching_terms const* t = op->off_diag_terms;
+  double* c = reinterpret_cast<double*>(coeffs);
+  offsets[0] = 0;
+  ptrdiff_t off = 0;
+  for (ptrdiff_t i = 0; i < batch_size; ++i) {
+    const uint64_t a = alphas[i];
+    for (int k = 0; k < t->number_terms; ++k) {
+      if ((a & t->m[k]) == t->r[k]) {
+        const int sign = 1 - 2 * (__builtin_popcountll(a & t->s[k]) % 2);
+        const double factor = xs != nullptr ? sign * xs[i] : (double)sign;
+        c[2 * off] = creal_of(t->v[k]) * factor;
+        c[2 * off + 1] = cimag_of(t->v[k]) * factor;
+        betas[off] = a ^ t->x[k];
+        ++off;
+      }
+    }
+    offsets[i + 1] = off;
+  }
+}
+
+// BatchedOperator.chpl:298-316
+extern "C" void ls_chpl_operator_apply_diag(ls_hs_operator* matrix, int64_t count, uint64_t* alphas,
+                                            chpl_external_array* coeffs, int64_t num_tasks) {
+  (void)num_tasks;
+  if (basis_number_bits(matrix->basis) > 64) {
+    ls_hs_error("bases with more than 64 bits are not yet implemented");
+    return;
+  }
+  if (matrix->basis->requires_projection) {
+    ls_hs_error("bases that require projection are not yet supported");
+    return;
+  }
+  double* cs = (double*)malloc(std::max<int64_t>(count, 1) * sizeof(double));
+  ls_internal_operator_apply_diag_x1(matrix, count, alphas, cs, nullptr);
+  coeffs->elts = cs;
+  coeffs->num_elts = (uint64_t)count;
+  coeffs->freer = (void*)&free_malloced;
+}
+
+// BatchedOperator.chpl:318-357
+extern "C" void ls_chpl_operator_apply_off_diag(ls_hs_operator* matrix, int64_t count, uint64_t* alphas,
+                                                chpl_external_array* betas, chpl_external_array* coeffs,
+                                                chpl_external_array* offsets, int64_t num_tasks) {
+  (void)num_tasks;
+  if (basis_number_bits(matrix->basis) > 64) {
+    ls_hs_error("bases with more than 64 bits are not yet implemented");
+    return;
+  }
+  const int nt = matrix->off_diag_terms ? matrix->off_diag_terms->number_terms : 0;
+  ptrdiff_t* offs = (ptrdiff_t*)calloc((size_t)count + 1, sizeof(ptrdiff_t));
+  if (nt != 0) {
+    uint64_t* bs = (uint64_t*)malloc(std::max<int64_t>(count * nt, 1) * 8);
+    ls_hs_scalar* cs = (ls_hs_scalar*)malloc(std::max<int64_t>(count * nt, 1) * 16);
+    ls_internal_operator_apply_off_diag_x1(matrix, count, alphas, bs, cs, offs, nullptr);
+    *betas = chpl_external_array{bs, (uint64_t)(count * nt), (void*)&free_malloced};
+    *coeffs = chpl_external_array{cs, (uint64_t)(count * nt), (void*)&free_malloced};
+  } else {
+    *betas = chpl_external_array{nullptr, 0, nullptr};
+    *coeffs = chpl_external_array{nullptr, 0, nullptr};
+  }
+  *offsets = chpl_external_array{offs, (uint64_t)count + 1, (void*)&free_malloced};
+}
+
+// =================================================================================================
+// Operators on the device
+// =================================================================================================
+namespace {
+
+struct TermTable {
+  int n = 0;
+  std::vector<uint64_t> m, l, r, x, s;
+  std::vector<double> v;  // interleaved
+};
+
+struct DeviceTermSet {
+  void* block = nullptr;
+  DeviceTerms terms;
+};
+
+struct OperatorCache {
+  TermTable off, diag;             // host copies (validated on every use)
+  DeviceTermSet fwd_off, adj_off, fwd_diag, adj_diag;
+  std::vector<int32_t> coupling;   // optional, per term (off then diag)
+  int32_t* d_coupling = nullptr;
+};
+
+std::unordered_map<const ls_hs_operator*, OperatorCache*> g_ops;
+
+TermTable read_terms(ls_hs_nonbranching_terms const* t) {
+  TermTable tt;
+  if (t == nullptr) return tt;
+  tt.n = t->number_terms;
+  tt.m.assign(t->m, t->m + tt.n);
+  tt.l.assign(t->l, t->l + tt.n);
+  tt.r.assign(t->r, t->r + tt.n);
+  tt.x.assign(t->x, t->x + tt.n);
+  tt.s.assign(t->s, t->s + tt.n);
+  const double* v = reinterpret_cast<const double*>(t->v);
+  tt.v.assign(v, v + 2 * (size_t)tt.n);
+  return tt;
+}
+
+bool same_terms(const TermTable& a, ls_hs_nonbranching_terms const* t) {
+  const int n = t ? t->number_terms : 0;
+  if (a.n != n) return false;
+  if (n == 0) return true;
+  return memcmp(a.m.data(), t->m, n * 8) == 0 && memcmp(a.l.data(), t->l, n * 8) == 0 &&
+         memcmp(a.r.data(), t->r, n * 8) == 0 && memcmp(a.x.data(), t->x, n * 8) == 0 &&
+         memcmp(a.s.data(), t->s, n * 8) == 0 &&
+         memcmp(a.v.data(), reinterpret_cast<const double*>(t->v), (size_t)n * 16) == 0;
+}
+
+// T^dagger: conj(v) (-1)^popcount(x & s), l and r exchanged.
+TermTable adjoint_terms(const TermTable& t) {
+  TermTable a = t;
+  for (int k = 0; k < t.n; ++k) {
+    std::swap(a.l[k], a.r[k]);
+    double sign = (__builtin_popcountll(t.x[k] & t.s[k]) & 1) ? -1.0 : 1.0;
+    a.v[2 * k] = sign * t.v[2 * k];
+    a.v[2 * k + 1] = -sign * t.v[2 * k + 1];
+  }
+  return a;
+}
+
+int upload_terms(const TermTable& t, DeviceTermSet* out) {
+  const size_t n = (size_t)std::max(t.n, 1);
+  const size_t bytes = n * (5 * 8 + 16);
+  std::vector<uint8_t> host(bytes, 0);
+  uint8_t* p = host.data();
+  auto put = [&](const void* src, size_t sz, size_t off) {
+    if (t.n > 0) memcpy(p + off, src, sz);
+  };
+  put(t.m.data(), t.n * 8, 0);
+  put(t.l.data(), t.n * 8, n * 8);
+  put(t.r.data(), t.n * 8, n * 16);
+  put(t.x.data(), t.n * 8, n * 24);
+  put(t.s.data(), t.n * 8, n * 32);
+  put(t.v.data(), t.n * 16, n * 40);
+  if (!cuda_ok(cudaMalloc(&out->block, bytes), "cudaMalloc(terms)")) return LS_GPU_ERR_CUDA;
+  if (!cuda_ok(cudaMemcpy(out->block, host.data(), bytes, cudaMemcpyHostToDevice), "upload terms"))
+    return LS_GPU_ERR_CUDA;
+  uint8_t* d = (uint8_t*)out->block;
+  out->terms.n = t.n;
+  out->terms.m = (const uint64_t*)(d);
+  out->terms.l = (const uint64_t*)(d + n * 8);
+  out->terms.r = (const uint64_t*)(d + n * 16);
+  out->terms.x = (const uint64_t*)(d + n * 24);
+  out->terms.s = (const uint64_t*)(d + n * 32);
+  out->terms.v = (const double2*)(d + n * 40);
+  return 0;
+}
+
+void free_cache(OperatorCache* c) {
+  for (DeviceTermSet* s : {&c->fwd_off, &c->adj_off, &c->fwd_diag, &c->adj_diag})
+    if (s->block) cudaFree(s->block);
+  if (c->d_coupling) cudaFree(c->d_coupling);
+  delete c;
+}
+
+OperatorCache* operator_cache(const ls_hs_operator* op) {
+  auto it = g_ops.find(op);
+  if (it != g_ops.end()) {
+    OperatorCache* c = it->second;
+    if (same_terms(c->off, op->off_diag_terms) && same_terms(c->diag, op->diag_terms)) return c;
+    free_cache(c);
+    g_ops.erase(it);
+  }
+  OperatorCache* c = new OperatorCache();
+  c->off = read_terms(op->off_diag_terms);
+  c->diag = read_terms(op->diag_terms);
+  if (upload_terms(c->off, &c->fwd_off) || upload_terms(adjoint_terms(c->off), &c->adj_off) ||
+      upload_terms(c->diag, &c->fwd_diag) || upload_terms(adjoint_terms(c->diag), &c->adj_diag)) {
+    free_cache(c);
+    return nullptr;
+  }
+  g_ops[op] = c;
+  return c;
+}
+
+int ensure_norms(IndexData* ix, const OrbitData* od) {
+  if (ix->d_norms != nullptr && ix->norms_for == od) return 0;
+  cudaStream_t s = default_stream();
+  if (ix->d_norms == nullptr &&
+      !cuda_ok(cudaMalloc((void**)&ix->d_norms, std::max<int64_t>(ix->n_states, 1) * 8), "cudaMalloc(norms)"))
+    return LS_GPU_ERR_CUDA;
+  int rc;
+  if (od != nullptr && od->n_elems > 0) {
+    const DeviceGroup* dg = orbit_device(od);
+    rc = dg ? launch_orbit_norms(*dg, ix->n_states, ix->d_reps, ix->d_norms, s) : LS_GPU_ERR_CUDA;
+  } else {
+    std::vector<double> ones((size_t)std::max<int64_t>(ix->n_states, 1), 1.0);
+    rc = cuda_ok(cudaMemcpyAsync(ix->d_norms, ones.data(), ones.size() * 8, cudaMemcpyHostToDevice, s),
+                 "norms") ? 0 : LS_GPU_ERR_CUDA;
+    if (rc == 0) rc = cuda_ok(cudaStreamSynchronize(s), "norms") ? 0 : LS_GPU_ERR_CUDA;
+  }
+  if (rc == 0) {
+    ix->norms_for = od;
+    ix->dev.norms = ix->d_norms;
+  }
+  return rc;
+}
+
+// Builds the kernel-side description of y = op x (adjoint: y = op^dagger x).
+int make_problem(ls_hs_operator const* op, bool adjoint, MatvecProblem* p) {
+  ls_hs_basis const* b = op->basis;
+  if (b == nullptr) return fail(LS_GPU_ERR_INVALID, "operator has no basis");
+  if (basis_number_bits(b) > 64) return fail(LS_GPU_ERR_INVALID, "bases with more than 64 bits are not yet implemented");
+  IndexData* ix = basis_index(b);
+  if (ix == nullptr) return fail(LS_GPU_ERR_NOT_BUILT, "basis is not built on the GPU");
+  const OrbitData* od = basis_orbit(b);
+  OperatorCache* c = operator_cache(op);
+  if (c == nullptr) return LS_GPU_ERR_CUDA;
+  p->projection = !b->requires_projection ? 0 : (has_permutations(b) ? 2 : 1);
+  if (p->projection == 1 && b->spin_inversion == 0) return fail(LS_GPU_ERR_INVALID, "projection without symmetries");
+  if (ensure_norms(ix, p->projection == 2 ? od : nullptr) != 0) return LS_GPU_ERR_CUDA;
+  p->group = DeviceGroup{};
+  if (p->projection == 2) {
+    const DeviceGroup* dg = orbit_device(od);
+    if (dg == nullptr) return LS_GPU_ERR_CUDA;
+    p->group = *dg;
+  }
+  p->group.spin_inversion = b->spin_inversion;
+  p->group.n_bits = basis_number_bits(b);
+  p->group.flip = low_ones(b->number_sites);
+  p->index = ix->dev;
+  // DistributedMatrixVector.chpl:105-113: identity index on one locale.
+  p->index.identity = b->state_index_is_identity ? 1 : 0;
+  // Without permutations a fixed-weight spin basis is a contiguous combinadic range starting at
+  // rank 0 (all states, or all states below the flipped maximum under spin inversion).
+  if (p->projection != 2 && !p->index.identity && b->particle_type == LS_HS_SPIN && b->number_up >= 0) {
+    p->index.combinadic = 1;
+    p->index.rank_base = 0;
+  }
+  p->constraint = basis_constraint(b);
+  p->off = adjoint ? c->adj_off.terms : c->fwd_off.terms;
+  p->diag = adjoint ? c->adj_diag.terms : c->fwd_diag.terms;
+  p->off.coupling = p->diag.coupling = c->d_coupling;
+  p->n_rows = ix->n_states;
+  return 0;
+}
+
+int read_and_clear_error(cudaStream_t s) {
+  int h[4] = {0, 0, 0, 0};
+  int* d = device_error_word();
+  if (!cuda_ok(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s), "read error word") ||
+      !cuda_ok(cudaMemsetAsync(d, 0, sizeof(h), s), "clear error word") ||
+      !cuda_ok(cudaStreamSynchronize(s), "matvec"))
+    return LS_GPU_ERR_CUDA;
+  if (h[0] != 0)
+    return fail(LS_GPU_ERR_BASIS,
+                "a generated basis state does not belong to the basis (the operator does not conserve "
+                "the basis' particle numbers)");
+  return 0;
+}
+
+}  // namespace
+
+// DistributedMatrixVector.chpl:1090-1105: y = H x on host arrays, one real vector.
+extern "C" void ls_chpl_matrix_vector_product(ls_hs_operator* matrix, int num_vectors, double const* x,
+                                              double* y) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (basis_number_bits(matrix->basis) > 64) {
+    ls_hs_error("bases with more than 64 bits are not yet implemented");
+    return;
+  }
+  if (num_vectors != 1) {
+    ls_hs_error("applying the Operator to more than 1 vector is not yet implemented");
+    return;
+  }
+  MatvecProblem p;
+  int rc = make_problem(matrix, false, &p);
+  if (rc != 0) {
+    report("ls_chpl_matrix_vector_product");
+    return;
+  }
+  const int64_t n = p.n_rows;
+  cudaStream_t s = default_stream();
+  double* d_x = (double*)scratch((size_t)std::max<int64_t>(n, 1) * 8, 4);
+  double* d_y = (double*)scratch((size_t)std::max<int64_t>(n, 1) * 8, 5);
+  if (!d_x || !d_y) {
+    report("ls_chpl_matrix_vector_product");
+    return;
+  }
+  if (n > 0) {
+    if (!cuda_ok(cudaMemcpyAsync(d_x, x, (size_t)n * 8, cudaMemcpyHostToDevice, s), "H2D x")) rc = LS_GPU_ERR_CUDA;
+    if (rc == 0) rc = launch_matvec(p, Scalar::Real, 1, d_x, 1, d_y, 1, device_error_word(), s);
+    if (rc == 0 && !cuda_ok(cudaMemcpyAsync(y, d_y, (size_t)n * 8, cudaMemcpyDeviceToHost, s), "D2H y"))
+      rc = LS_GPU_ERR_CUDA;
+    if (rc == 0) rc = read_and_clear_error(s);
+  }
+  if (rc != 0) report("ls_chpl_matrix_vector_product");
+}
+
+// =================================================================================================
+// Additive API
+// =================================================================================================
+extern "C" int ls_gpu_basis_info(ls_hs_basis const* basis, int64_t* number_states,
+                                 uint64_t const** d_representatives, double const** d_norms) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  IndexData* ix = basis_index(basis);
+  if (ix == nullptr) return fail(LS_GPU_ERR_NOT_BUILT, "basis is not built on the GPU");
+  const OrbitData* od = has_permutations(basis) ? basis_orbit(basis) : nullptr;
+  if (ensure_norms(ix, od) != 0) return LS_GPU_ERR_CUDA;
+  if (number_states) *number_states = ix->n_states;
+  if (d_representatives) *d_representatives = ix->d_reps;
+  if (d_norms) *d_norms = ix->d_norms;
+  return 0;
+}
+
+static int gpu_matvec(ls_hs_operator const* op, Scalar sc, int k, double const* d_x, int64_t ldx,
+                      double* d_y, int64_t ldy, int adjoint, void* stream) {
+  if (k < 0 || ldx < k || ldy < k) return fail(LS_GPU_ERR_INVALID, "invalid k / leading dimension");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  MatvecProblem p;
+  int rc = make_problem(op, adjoint != 0, &p);
+  if (rc != 0) return rc;
+  cudaStream_t s = stream ? (cudaStream_t)stream : default_stream();
+  rc = launch_matvec(p, sc, k, d_x, ldx, d_y, ldy, device_error_word(), s);
+  if (rc != 0) return rc;
+  return read_and_clear_error(s);
+}
+
+extern "C" int ls_gpu_matvec_c128(ls_hs_operator const* op, int k, double const* d_x, int64_t ldx,
+                                  double* d_y, int64_t ldy, int adjoint, void* stream) {
+  return gpu_matvec(op, Scalar::Complex, k, d_x, ldx, d_y, ldy, adjoint, stream);
+}
+
+extern "C" int ls_gpu_matvec_f64(ls_hs_operator const* op, int k, double const* d_x, int64_t ldx,
+                                 double* d_y, int64_t ldy, int adjoint, void* stream) {
+  return gpu_matvec(op, Scalar::Real, k, d_x, ldx, d_y, ldy, adjoint, stream);
+}
+
+extern "C" int ls_gpu_state_info(ls_hs_basis const* basis, int64_t batch, uint64_t const* d_alphas,
+                                 uint64_t* d_betas, double* d_characters, double* d_norms, void* stream) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  const OrbitData* od = basis_orbit(basis);
+  if (od == nullptr || od->n_elems == 0) return fail(LS_GPU_ERR_INVALID, "basis has no symmetry group on the GPU");
+  cudaStream_t s = stream ? (cudaStream_t)stream : default_stream();
+  const DeviceGroup* dg = orbit_device(od);
+  if (dg == nullptr) return LS_GPU_ERR_CUDA;
+  return launch_state_info(*dg, batch, d_alphas, d_betas, (double2*)d_characters, d_norms, 8, s);
+}
+
+extern "C" int ls_gpu_is_representative(ls_hs_basis const* basis, int64_t batch, uint64_t const* d_alphas,
+                                        uint8_t* d_flags, double* d_norms, void* stream) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  const OrbitData* od = basis_orbit(basis);
+  if (od == nullptr || od->n_elems == 0) return fail(LS_GPU_ERR_INVALID, "basis has no symmetry group on the GPU");
+  cudaStream_t s = stream ? (cudaStream_t)stream : default_stream();
+  const DeviceGroup* dg = orbit_device(od);
+  if (dg == nullptr) return LS_GPU_ERR_CUDA;
+  return launch_is_representative(*dg, batch, d_alphas, d_flags, d_norms, 4, s);
+}
+
+extern "C" int ls_gpu_state_index(ls_hs_basis const* basis, int64_t batch, uint64_t const* d_alphas,
+                                  int64_t* d_indices, void* stream) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  IndexData* ix = basis_index(basis);
+  if (ix == nullptr) return fail(LS_GPU_ERR_NOT_BUILT, "basis is not built on the GPU");
+  cudaStream_t s = stream ? (cudaStream_t)stream : default_stream();
+  return launch_state_index(ix->dev, batch, d_alphas, d_indices, s);
+}
+
+extern "C" int ls_gpu_coupling_inner_products(ls_hs_operator const* op, int n_couplings,
+                                              int32_t const* term_coupling, double const* d_g,
+                                              double const* d_x, double* d_out, void* stream) {
+  (void)op; (void)n_couplings; (void)term_coupling; (void)d_g; (void)d_x; (void)d_out; (void)stream;
+  return fail(LS_GPU_ERR_INVALID, "not implemented yet");
+}
+
+extern "C" int ls_gpu_matvec_multi_sector_c128(int n_sectors, ls_hs_operator const* const* ops, int k,
+                                               double const* const* d_x, double* const* d_y, int adjoint,
+                                               void* stream) {
+  for (int i = 0; i < n_sectors; ++i) {
+    int rc = ls_gpu_matvec_c128(ops[i], k, d_x[i], k, d_y[i], k, adjoint, stream);
+    if (rc != 0) return rc;
+  }
+  return 0;
+}

@@ -1,0 +1,169 @@
+// lsg.h -- internal declarations shared by the CUDA kernels and the C-ABI layer of
+// libls_gb300.so.  Nothing here is part of the public ABI (see include/ls_gb300.h).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "ls_gb300.h"
+
+namespace lsg {
+
+constexpr int kMaxGroupElements = 2048;  // |G| handled by the device orbit scan
+constexpr int kWarp = 32;
+
+// Device view of a permutation group (all pointers are device memory).
+struct DeviceGroup {
+  int n_bits = 0;          // bits of a basis state
+  int n_elems = 0;         // |G| (0: spin inversion only / no projection)
+  int depth = 0;           // Benes stages
+  int spin_inversion = 0;  // 0, +1, -1
+  uint64_t flip = 0;       // all n_bits set
+  const uint64_t* masks_t = nullptr;  // [n_elems][depth] (transposed reference layout)
+  const uint32_t* shifts = nullptr;   // [depth]
+  const double2* chars = nullptr;     // [n_elems] characters
+  const uint64_t* onehot = nullptr;   // [n_bits][n_elems]: image of the one-bit state 1<<b under g
+  const uint16_t* prio = nullptr;     // [n_elems] tie-break priority of state_info (lane order)
+};
+
+// Device view of a sorted representative array and its prefix-bucket index.
+struct DeviceIndex {
+  int64_t n_states = 0;
+  const uint64_t* reps = nullptr;
+  const double* norms = nullptr;      // state_info norms of the representatives
+  const int64_t* offsets = nullptr;   // [2^prefix_bits] window starts (clamped), or null
+  int shift = 0;                      // bucket = state >> shift
+  int64_t range_size = 0;             // window length
+  int prefix_bits = 0;
+  int identity = 0;                   // index(state) = state
+  // combinadics ranking (fixed Hamming weight, no projection): index = rank(state) - rank_base
+  int combinadic = 0;
+  int64_t rank_base = 0;
+};
+
+// Basis-level constraints checked on every generated state (fixed particle numbers).
+struct DeviceConstraint {
+  int kind = 0;            // 0 none, 1 popcount(state) == w0, 2 popcount(low half)==w0 && popcount(high half)==w1
+  int half_bits = 0;
+  int w0 = 0, w1 = 0;
+};
+
+// Off-diagonal / diagonal term tables on the device.
+struct DeviceTerms {
+  int n = 0;
+  const uint64_t* m = nullptr;
+  const uint64_t* l = nullptr;  // pattern matched by the row state (the bra side)
+  const uint64_t* r = nullptr;
+  const uint64_t* x = nullptr;
+  const uint64_t* s = nullptr;
+  const double2* v = nullptr;
+  const int32_t* coupling = nullptr;  // optional coupling id per term
+};
+
+// Host-side records behind the opaque kernel-data pointers of the plugin tables.
+struct OrbitData {
+  uint32_t magic;
+  int n_bits, n_elems, depth, spin_inversion;
+  std::vector<uint64_t> masks;        // reference layout [depth][n_elems]
+  std::vector<uint32_t> shifts;
+  std::vector<double> chars_re, chars_im;
+  // Host image of the device block (masks_t | shifts | chars | onehot | prio) and its offsets;
+  // uploaded on first use so that kernel data can be created on a machine without a GPU.
+  std::vector<uint8_t> host_block;
+  size_t off_masks = 0, off_shifts = 0, off_chars = 0, off_onehot = 0, off_prio = 0;
+  bool standard_shifts = true;
+  mutable DeviceGroup dev;
+  mutable void* dev_block = nullptr;  // one allocation holding all device arrays
+  mutable int dev_device = -1;
+};
+
+struct IndexData {
+  uint32_t magic;
+  int64_t n_states;
+  const uint64_t* host_reps;          // borrowed from the basis (chpl_external_array)
+  int number_bits;
+  int prefix_bits;
+  DeviceIndex dev;
+  uint64_t* d_reps = nullptr;
+  int64_t* d_offsets = nullptr;
+  double* d_norms = nullptr;          // filled lazily when a projected matvec needs them
+  const OrbitData* norms_for = nullptr;
+};
+
+constexpr uint32_t kOrbitMagic = 0x4f524249u;  // "ORBI"
+constexpr uint32_t kIndexMagic = 0x494e4458u;  // "INDX"
+
+// ---- runtime (abi.cu) --------------------------------------------------------------------------
+cudaStream_t default_stream();
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);  // records msg, returns code
+bool cuda_ok(cudaError_t e, const char* what);
+int* device_error_word();                     // 4 ints of device scratch for kernel error reports
+void* scratch(size_t bytes, int slot);        // cached device scratch buffers
+void* pinned_scratch(size_t bytes, int slot); // cached pinned host buffers
+int num_sms();
+
+// ---- orbit scan + enumeration + index (basis.cu) -----------------------------------------------
+int launch_state_info(const DeviceGroup& g, int64_t n, const uint64_t* d_x, uint64_t* d_rep,
+                      double2* d_char, double* d_norm, int lane_width, cudaStream_t s);
+int launch_is_representative(const DeviceGroup& g, int64_t n, const uint64_t* d_x,
+                             uint8_t* d_flag, double* d_norm, int lane_width, cudaStream_t s);
+int launch_orbit_norms(const DeviceGroup& g, int64_t n, const uint64_t* d_reps, double* d_norms,
+                       cudaStream_t s);
+int compute_site_images(OrbitData* od);          // host tables (no GPU needed)
+const DeviceGroup* orbit_device(const OrbitData* od);  // uploads on first use; null on failure
+
+struct EnumerateRequest {
+  int mode;              // 0 projected spin, 1 unprojected (fixed weight or all), 2 spinful per sector
+  int hamming_fixed;
+  int number_sites;
+  int spin_inversion;
+  uint64_t lower, upper;
+  int reference_norm_rule;  // 1: keep a state iff the reference's floating stabiliser sum > 0
+};
+// Enumerates into device memory; *d_out is allocated with cudaMalloc (caller frees).
+int enumerate_states(const DeviceGroup* g, const EnumerateRequest& req, uint64_t** d_out,
+                     int64_t* count, cudaStream_t s);
+
+int build_prefix_index(const uint64_t* d_reps, int64_t n, int number_bits, int prefix_bits,
+                       int64_t** d_offsets, int64_t* range_size, int* shift, cudaStream_t s);
+int launch_state_index(const DeviceIndex& ix, int64_t n, const uint64_t* d_x, int64_t* d_out,
+                       cudaStream_t s);
+
+// combinadics on the host (Basis.hs:519-550)
+int64_t fixed_hamming_state_to_index(uint64_t a);
+uint64_t fixed_hamming_index_to_state(int64_t index, int h);
+
+// ---- matvec (matvec.cu) ------------------------------------------------------------------------
+enum class Scalar { Real, Complex };
+
+struct MatvecProblem {
+  int projection;            // 0 none, 1 spin inversion only, 2 full group
+  DeviceGroup group;
+  DeviceIndex index;
+  DeviceConstraint constraint;
+  DeviceTerms off;           // terms applied to the row state through their l pattern
+  DeviceTerms diag;
+  int64_t n_rows;
+};
+
+int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, int64_t ldx,
+                  double* d_y, int64_t ldy, int* d_err, cudaStream_t s);
+
+struct MultiSectorProblem {
+  int n_sectors;
+  const MatvecProblem* problems;   // host array
+  int k;
+  const double* const* d_x;        // host array of device pointers
+  double* const* d_y;
+};
+int launch_matvec_multi(const MultiSectorProblem& mp, int* d_err, cudaStream_t s);
+
+int launch_coupling_products(const MatvecProblem& p, int n_couplings, const double* d_g,
+                             const double* d_x, double* d_out, int* d_err, cudaStream_t s);
+
+}  // namespace lsg

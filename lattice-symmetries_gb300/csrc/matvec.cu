@@ -1,0 +1,97 @@
+// matvec.cu -- launch policy of the gather kernels (kernel choice, grid shape, RHS blocking).
+#include <algorithm>
+
+#include "matvec_dispatch.h"
+#include "matvec_impl.cuh"
+
+namespace lsg {
+
+int launch_projected_cplx_k1(int, bool, const MatvecProblem&, const SmemLayout&, LaunchShape,
+                             const double*, int64_t, double*, int64_t, int*, const uint64_t*,
+                             cudaStream_t);
+int launch_projected_cplx_k4(int, bool, const MatvecProblem&, const SmemLayout&, LaunchShape,
+                             const double*, int64_t, double*, int64_t, int*, const uint64_t*,
+                             cudaStream_t);
+int launch_projected_cplx_k8(int, bool, const MatvecProblem&, const SmemLayout&, LaunchShape,
+                             const double*, int64_t, double*, int64_t, int*, const uint64_t*,
+                             cudaStream_t);
+int launch_projected_cplx_k16(int, bool, const MatvecProblem&, const SmemLayout&, LaunchShape,
+                              const double*, int64_t, double*, int64_t, int*, const uint64_t*,
+                              cudaStream_t);
+
+int launch_projected_cplx(int gpl, bool inv, int k, const MatvecProblem& p, const SmemLayout& L,
+                          LaunchShape sh, const double* x, int64_t ldx, double* y, int64_t ldy,
+                          int* err, const uint64_t* binom, cudaStream_t s) {
+  switch (k) {
+    case 1: return launch_projected_cplx_k1(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
+    case 4: return launch_projected_cplx_k4(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
+    case 8: return launch_projected_cplx_k8(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
+    case 16: return launch_projected_cplx_k16(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
+    default: return LS_GPU_ERR_INVALID;
+  }
+}
+
+static int g_threads_override = 0;
+static int g_blocks_per_sm_override = 0;
+
+int set_matvec_config(int threads, int blocks_per_sm) {
+  g_threads_override = threads;
+  g_blocks_per_sm_override = blocks_per_sm;
+  return 0;
+}
+
+static int pick_gpl(int n_elems) {
+  const int need = (n_elems + 31) / 32;
+  for (int g : kGplChoices)
+    if (g >= need) return g;
+  return -1;
+}
+
+extern const uint64_t* device_binomials();
+
+// Splits k right-hand sides into launches of 16, 8, 4 and 1 columns.
+int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, int64_t ldx,
+                  double* d_y, int64_t ldy, int* d_err, cudaStream_t s) {
+  if (p.n_rows == 0 || k == 0) return 0;
+  const uint64_t* binom = device_binomials();
+  if (binom == nullptr) return LS_GPU_ERR_CUDA;
+  const bool cplx = sc == Scalar::Complex;
+  const size_t scalar_words = cplx ? 2 : 1;  // doubles per element
+  if (p.projection == 2) {
+    const int gpl = pick_gpl(p.group.n_elems);
+    if (gpl < 0) return fail(LS_GPU_ERR_INVALID, "symmetry group too large for the matvec kernels");
+    const SmemLayout L = make_layout(p, true);
+    if (L.total > 200 * 1024) return fail(LS_GPU_ERR_INVALID, "term tables too large for shared memory");
+    const int threads = g_threads_override > 0 ? g_threads_override : 256;
+    const int warps_per_block = threads / 32;
+    const int bps = g_blocks_per_sm_override > 0 ? g_blocks_per_sm_override : 2;
+    int64_t blocks = (int64_t)num_sms() * bps * 4;  // several waves for load balance
+    blocks = std::min<int64_t>(blocks, (p.n_rows + warps_per_block - 1) / warps_per_block);
+    blocks = std::max<int64_t>(blocks, 1);
+    const LaunchShape sh{(int)blocks, threads};
+    const bool inv = p.group.spin_inversion != 0;
+    int done = 0;
+    while (done < k) {
+      const int left = k - done;
+      int chunk = 1;
+      if (cplx) chunk = left >= 16 ? 16 : left >= 8 ? 8 : left >= 4 ? 4 : 1;
+      const double* xs = d_x + (size_t)done * scalar_words;
+      double* ys = d_y + (size_t)done * scalar_words;
+      int rc = cplx ? launch_projected_cplx(gpl, inv, chunk, p, L, sh, xs, ldx, ys, ldy, d_err, binom, s)
+                    : launch_projected_real(gpl, inv, p, L, sh, xs, ldx, ys, ldy, d_err, binom, s);
+      if (rc != 0) return rc;
+      done += chunk;
+    }
+    return 0;
+  }
+  const SmemLayout L = make_layout(p, false);
+  if (L.total > 200 * 1024) return fail(LS_GPU_ERR_INVALID, "term tables too large for shared memory");
+  const int threads = 256;
+  int64_t blocks = (p.n_rows + threads - 1) / threads;
+  blocks = std::min<int64_t>(blocks, (int64_t)num_sms() * 16);
+  blocks = std::max<int64_t>(blocks, 1);
+  const LaunchShape sh{(int)blocks, threads};
+  return launch_plain(cplx, p.projection == 1, k, p, L, sh, d_x, ldx, d_y, ldy, d_err, binom, s);
+}
+
+}  // namespace lsg

@@ -1,0 +1,415 @@
+// matvec_impl.cuh -- gather-form H*x kernels (included by the matvec_*.cu translation units,
+// each of which instantiates a subset so that the build compiles in parallel).
+//
+// The reference computes y = H x by scattering: every representative alpha_j generates
+// beta = alpha_j ^ x_t, projects it onto its representative and adds
+// chi * v * sign * x_j * n(beta)/n(alpha_j) to y[index(rep(beta))] with atomics
+// (chapel/src/BatchedOperator.chpl:207-253, DistributedMatrixVector.chpl:91-143).
+//
+// Here every output row gathers instead.  For a row state a = alpha_i and a term t with
+// (a & m_t) == l_t, the column state is beta = a ^ x_t and
+//
+//     H[i, j] += v_t (-1)^popcount(beta & s_t) conj(chi(g)) n_j / n_i,   alpha_j = g.beta,
+//
+// the same matrix element the reference produces from column j (it is <alpha_i-bar|H|alpha_j-bar>
+// in the orthonormal symmetrised basis).  No atomics, deterministic summation order.  H^dagger
+// uses the same kernels with the adjoint term table.
+//
+// Projected bases: one warp per row.  Lane L owns group elements e = L + 32k (k < GPL) and keeps
+// g.a in registers; because permuting bits is linear over XOR, g.beta = g.a ^ g.x_t, and g.x_t
+// is an XOR of one-hot site images (a shared-memory table [bit][element]).  The warp reduces the
+// candidates (and their spin-flipped partners) to the representative with three REDUX.MIN
+// steps, and every 32 targets the lanes look up indices and gather x in parallel.
+#pragma once
+
+#include "lsg.h"
+
+namespace lsg {
+
+__device__ __forceinline__ bool constraint_ok(const DeviceConstraint& c, uint64_t s) {
+  if (c.kind == 0) return true;
+  if (c.kind == 1) return __popcll(s) == c.w0;
+  const uint64_t lo = s & ((c.half_bits >= 64) ? ~0ull : ((1ull << c.half_bits) - 1));
+  return __popcll(lo) == c.w0 && __popcll(s >> c.half_bits) == c.w1;
+}
+
+// Index lookup (duplicated from basis.cu as a header-local function so that each matvec
+// translation unit inlines it).
+__device__ __forceinline__ int64_t mv_index_lookup(const DeviceIndex& ix, uint64_t needle,
+                                                   const uint64_t* __restrict__ binom /*65x65*/) {
+  if (ix.identity) return (int64_t)needle;
+  if (ix.combinadic) {
+    int64_t i = 0;
+    uint64_t a = needle;
+    for (int k = 1; a != 0; ++k) {
+      const int c = __ffsll((long long)a) - 1;
+      a &= a - 1;
+      i += (c <= 0 || k > c) ? 0 : (int64_t)__ldg(binom + c * 65 + k);
+    }
+    return i - ix.rank_base;
+  }
+  int64_t len = ix.range_size;
+  if (len <= 0) return -1;
+  int64_t base = __ldg(ix.offsets + (needle >> ix.shift));
+  while (len > 1) {
+    const int64_t half = len >> 1;
+    base = (__ldg(ix.reps + base + half) < needle) ? base + half : base;
+    len -= half;
+  }
+  if (base < ix.n_states && __ldg(ix.reps + base) < needle) ++base;
+  return (base < ix.n_states && __ldg(ix.reps + base) == needle) ? base : -1;
+}
+
+struct C2 {
+  double re, im;
+};
+__device__ __forceinline__ C2 cmul(C2 a, C2 b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+__device__ __forceinline__ C2 cmul_conj_b(C2 a, C2 b) {  // a * conj(b)
+  return {a.re * b.re + a.im * b.im, a.im * b.re - a.re * b.im};
+}
+
+// Shared-memory layout of the projected kernel.
+struct SmemLayout {
+  int onehot_in_smem;
+  size_t off_onehot, off_chars, off_tm, off_tl, off_tx, off_ts, off_tv, off_dm, off_dr, off_ds, off_dv;
+  size_t total;
+};
+
+inline SmemLayout make_layout(const MatvecProblem& p, bool with_group) {
+  SmemLayout L{};
+  auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  size_t o = 0;
+  const int G = with_group ? p.group.n_elems : 0;
+  const size_t onehot_bytes = with_group ? (size_t)p.group.n_bits * G * 8 : 0;
+  L.off_chars = o; o = al(o + (size_t)G * 16);
+  L.off_tm = o; o = al(o + (size_t)p.off.n * 8);
+  L.off_tl = o; o = al(o + (size_t)p.off.n * 8);
+  L.off_tx = o; o = al(o + (size_t)p.off.n * 8);
+  L.off_ts = o; o = al(o + (size_t)p.off.n * 8);
+  L.off_tv = o; o = al(o + (size_t)p.off.n * 16);
+  L.off_dm = o; o = al(o + (size_t)p.diag.n * 8);
+  L.off_dr = o; o = al(o + (size_t)p.diag.n * 8);
+  L.off_ds = o; o = al(o + (size_t)p.diag.n * 8);
+  L.off_dv = o; o = al(o + (size_t)p.diag.n * 16);
+  // One-hot table last; kept in shared memory when the whole layout stays under 112 KB
+  // (two CTAs per SM), otherwise read through L1 from global memory.
+  L.off_onehot = o;
+  if (with_group && o + onehot_bytes <= 112 * 1024) {
+    L.onehot_in_smem = 1;
+    o = al(o + onehot_bytes);
+  } else {
+    L.onehot_in_smem = 0;
+  }
+  L.total = o;
+  return L;
+}
+
+__device__ __forceinline__ void stage_u64(uint64_t* dst, const uint64_t* src, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+__device__ __forceinline__ void stage_d2(double2* dst, const double2* src, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
+struct Staged {
+  const uint64_t* onehot;
+  const double2* chars;
+  const uint64_t *tm, *tl, *tx, *ts;
+  const double2* tv;
+  const uint64_t *dm, *dr, *ds;
+  const double2* dv;
+};
+
+__device__ __forceinline__ Staged stage_problem(const MatvecProblem& p, const SmemLayout& L,
+                                                unsigned char* smem, bool with_group) {
+  Staged S;
+  uint64_t* tm = (uint64_t*)(smem + L.off_tm);
+  uint64_t* tl = (uint64_t*)(smem + L.off_tl);
+  uint64_t* tx = (uint64_t*)(smem + L.off_tx);
+  uint64_t* ts = (uint64_t*)(smem + L.off_ts);
+  double2* tv = (double2*)(smem + L.off_tv);
+  uint64_t* dm = (uint64_t*)(smem + L.off_dm);
+  uint64_t* dr = (uint64_t*)(smem + L.off_dr);
+  uint64_t* ds = (uint64_t*)(smem + L.off_ds);
+  double2* dv = (double2*)(smem + L.off_dv);
+  stage_u64(tm, p.off.m, p.off.n);
+  stage_u64(tl, p.off.l, p.off.n);
+  stage_u64(tx, p.off.x, p.off.n);
+  stage_u64(ts, p.off.s, p.off.n);
+  stage_d2(tv, p.off.v, p.off.n);
+  stage_u64(dm, p.diag.m, p.diag.n);
+  stage_u64(dr, p.diag.r, p.diag.n);
+  stage_u64(ds, p.diag.s, p.diag.n);
+  stage_d2(dv, p.diag.v, p.diag.n);
+  S.tm = tm; S.tl = tl; S.tx = tx; S.ts = ts; S.tv = tv;
+  S.dm = dm; S.dr = dr; S.ds = ds; S.dv = dv;
+  if (with_group) {
+    double2* ch = (double2*)(smem + L.off_chars);
+    stage_d2(ch, p.group.chars, p.group.n_elems);
+    S.chars = ch;
+    if (L.onehot_in_smem) {
+      uint64_t* oh = (uint64_t*)(smem + L.off_onehot);
+      stage_u64(oh, p.group.onehot, p.group.n_bits * p.group.n_elems);
+      S.onehot = oh;
+    } else {
+      S.onehot = p.group.onehot;
+    }
+  } else {
+    S.chars = nullptr;
+    S.onehot = nullptr;
+  }
+  __syncthreads();
+  return S;
+}
+
+struct Acc {
+  double re = 0.0, im = 0.0;  // the real kernels use re only
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+  return v;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Projected kernel: K right-hand sides (K in {1, 4, 8, 16}), GPL group elements per lane.
+// x, y: row-major [rows][ld] of double (real) or double2 (complex, CPLX).
+// ------------------------------------------------------------------------------------------------
+template <int GPL, bool INV, bool CPLX, int K>
+__global__ void __launch_bounds__(256, 2)
+    k_matvec_projected(const MatvecProblem p, const SmemLayout L, const double* __restrict__ x,
+                       int64_t ldx, double* __restrict__ y, int64_t ldy, int* __restrict__ err,
+                       const uint64_t* __restrict__ binom) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Staged S = stage_problem(p, L, smem, true);
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int Q = 32 / K;  // slots handled per flush round
+  const int lane = threadIdx.x & 31;
+  const int G = p.group.n_elems;
+  const int nbits = p.group.n_bits;
+  const uint64_t flip = p.group.flip;
+  const int rhs = lane % K;   // my right-hand side in the flush
+  const int q = lane / K;     // my slot offset in a flush round
+  const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+
+  int eidx[GPL];
+  bool evalid[GPL];
+#pragma unroll
+  for (int k = 0; k < GPL; ++k) {
+    const int e = lane + 32 * k;
+    evalid[k] = e < G;
+    eidx[k] = evalid[k] ? e : (G - 1);
+  }
+
+  for (int64_t row = warp_id; row < p.n_rows; row += n_warps) {
+    const uint64_t a = __ldg(p.index.reps + row);
+    const double na = __ldg(p.index.norms + row);
+
+    // g.a for my elements
+    uint64_t ga[GPL];
+#pragma unroll
+    for (int k = 0; k < GPL; ++k) ga[k] = 0;
+    for (uint64_t bits = a; bits != 0; bits &= bits - 1) {
+      const uint64_t* oh = S.onehot + (int64_t)(__ffsll((long long)bits) - 1) * G;
+#pragma unroll
+      for (int k = 0; k < GPL; ++k) ga[k] ^= oh[eidx[k]];
+    }
+
+    // diagonal: lanes split the terms, warp sum
+    double dre = 0.0, dim = 0.0;
+    for (int t = lane; t < p.diag.n; t += 32) {
+      if ((a & S.dm[t]) == S.dr[t]) {
+        const double2 v = S.dv[t];
+        const bool neg = __popcll(a & S.ds[t]) & 1;
+        dre += neg ? -v.x : v.x;
+        if constexpr (CPLX) dim += neg ? -v.y : v.y;
+      }
+    }
+    dre = warp_sum(dre);
+    if constexpr (CPLX) dim = warp_sum(dim);
+
+    Acc acc;
+    uint64_t my_rep = ~0ull;
+    uint32_t my_idx = 0;
+    double2 my_c = make_double2(0.0, 0.0);
+    int nslot = 0;
+
+    auto flush = [&]() {
+      // every lane with a slot: index, character, norm ratio -> complex factor
+      int64_t j = -1;
+      double fre = 0.0, fim = 0.0;
+      if (lane < nslot) {
+        j = mv_index_lookup(p.index, my_rep, binom);
+        if (j >= 0) {
+          double2 chi = S.chars[my_idx >> 1];
+          if (INV && (my_idx & 1) && p.group.spin_inversion == -1) chi = make_double2(-chi.x, -chi.y);
+          const double ratio = __ldg(p.index.norms + j) / na;
+          const C2 f = cmul_conj_b(C2{my_c.x, my_c.y}, C2{chi.x, chi.y});
+          fre = f.re * ratio;
+          fim = f.im * ratio;
+        }
+      }
+      for (int s0 = 0; s0 < nslot; s0 += Q) {
+        const int s = s0 + q;
+        const int src = s & 31;
+        const int64_t js = (K == 1) ? j : __shfl_sync(FULL, j, src);
+        const double sre = (K == 1) ? fre : __shfl_sync(FULL, fre, src);
+        const double sim = (K == 1) ? fim : __shfl_sync(FULL, fim, src);
+        if (s < nslot && js >= 0) {
+          if constexpr (CPLX) {
+            const double2 xv = __ldg(reinterpret_cast<const double2*>(x) + js * ldx + rhs);
+            acc.re += sre * xv.x - sim * xv.y;
+            acc.im += sre * xv.y + sim * xv.x;
+          } else {
+            const double xv = __ldg(x + js * ldx + rhs);
+            acc.re += sre * xv;
+          }
+        }
+        if (K == 1) break;
+      }
+    };
+
+    for (int t = 0; t < p.off.n; ++t) {
+      if ((a & S.tm[t]) != S.tl[t]) continue;
+      const uint64_t xt = S.tx[t];
+      const uint64_t beta = a ^ xt;
+      if (!constraint_ok(p.constraint, beta)) {
+        if (lane == 0) atomicOr(err, 1);
+        continue;
+      }
+      double2 c = S.tv[t];
+      if (__popcll(beta & S.ts[t]) & 1) c = make_double2(-c.x, -c.y);
+
+      uint64_t gx[GPL];
+#pragma unroll
+      for (int k = 0; k < GPL; ++k) gx[k] = ga[k];
+      for (uint64_t bits = xt; bits != 0; bits &= bits - 1) {
+        const uint64_t* oh = S.onehot + (int64_t)(__ffsll((long long)bits) - 1) * G;
+#pragma unroll
+        for (int k = 0; k < GPL; ++k) gx[k] ^= oh[eidx[k]];
+      }
+      uint64_t best = ~0ull;
+      uint32_t bidx = 0xffffffffu;
+#pragma unroll
+      for (int k = 0; k < GPL; ++k) {
+        uint64_t cand = gx[k];
+        uint32_t id = 2u * (uint32_t)(lane + 32 * k);
+        if (INV) {
+          const uint64_t top = (cand >> (nbits - 1)) & 1ull;
+          cand ^= flip & (0ull - top);
+          id += (uint32_t)top;
+        }
+        if (evalid[k] && cand < best) {
+          best = cand;
+          bidx = id;
+        }
+      }
+      const uint32_t hi = (uint32_t)(best >> 32), lo = (uint32_t)best;
+      const uint32_t mhi = __reduce_min_sync(FULL, hi);
+      const uint32_t mlo = __reduce_min_sync(FULL, hi == mhi ? lo : 0xffffffffu);
+      const uint32_t midx = __reduce_min_sync(FULL, (hi == mhi && lo == mlo) ? bidx : 0xffffffffu);
+      if (lane == nslot) {
+        my_rep = ((uint64_t)mhi << 32) | mlo;
+        my_idx = midx;
+        my_c = c;
+      }
+      if (++nslot == 32) {
+        flush();
+        nslot = 0;
+      }
+    }
+    if (nslot > 0) flush();
+
+    // reduce lanes holding the same right-hand side, add the diagonal, store
+    if constexpr (CPLX) {
+#pragma unroll
+      for (int d = 16; d >= K; d >>= 1) {
+        acc.re += __shfl_xor_sync(FULL, acc.re, d);
+        acc.im += __shfl_xor_sync(FULL, acc.im, d);
+      }
+      if (lane < K) {
+        const double2 xi = __ldg(reinterpret_cast<const double2*>(x) + row * ldx + lane);
+        double2 out;
+        out.x = acc.re + (dre * xi.x - dim * xi.y);
+        out.y = acc.im + (dre * xi.y + dim * xi.x);
+        reinterpret_cast<double2*>(y)[row * ldy + lane] = out;
+      }
+    } else {
+#pragma unroll
+      for (int d = 16; d >= K; d >>= 1) acc.re += __shfl_xor_sync(FULL, acc.re, d);
+      if (lane < K) y[row * ldy + lane] = acc.re + dre * __ldg(x + row * ldx + lane);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Unprojected / spin-inversion-only kernel: one thread per row.
+// ------------------------------------------------------------------------------------------------
+template <bool CPLX, bool INV>
+__global__ void __launch_bounds__(256)
+    k_matvec_plain(const MatvecProblem p, const SmemLayout L, const double* __restrict__ x,
+                   int64_t ldx, double* __restrict__ y, int64_t ldy, int k_rhs,
+                   int* __restrict__ err, const uint64_t* __restrict__ binom) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Staged S = stage_problem(p, L, smem, false);
+  const uint64_t flip = p.group.flip;
+  const double chi_flip = (double)p.group.spin_inversion;
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < p.n_rows;
+       row += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t a = (p.index.identity) ? (uint64_t)row : __ldg(p.index.reps + row);
+    double dre = 0.0, dim = 0.0;
+    for (int t = 0; t < p.diag.n; ++t) {
+      if ((a & S.dm[t]) == S.dr[t]) {
+        const double2 v = S.dv[t];
+        const bool neg = __popcll(a & S.ds[t]) & 1;
+        dre += neg ? -v.x : v.x;
+        dim += neg ? -v.y : v.y;
+      }
+    }
+    for (int r = 0; r < k_rhs; ++r) {
+      double are = 0.0, aim = 0.0;
+      if constexpr (CPLX) {
+        const double2 xi = reinterpret_cast<const double2*>(x)[row * ldx + r];
+        are = dre * xi.x - dim * xi.y;
+        aim = dre * xi.y + dim * xi.x;
+      } else {
+        are = dre * x[row * ldx + r];
+      }
+      for (int t = 0; t < p.off.n; ++t) {
+        if ((a & S.tm[t]) != S.tl[t]) continue;
+        uint64_t beta = a ^ S.tx[t];
+        if (!constraint_ok(p.constraint, beta)) {
+          atomicOr(err, 1);
+          continue;
+        }
+        double2 c = S.tv[t];
+        if (__popcll(beta & S.ts[t]) & 1) c = make_double2(-c.x, -c.y);
+        if (INV) {
+          const uint64_t inv = beta ^ flip;
+          if (inv < beta) {
+            beta = inv;
+            c = make_double2(c.x * chi_flip, c.y * chi_flip);
+          }
+        }
+        const int64_t j = mv_index_lookup(p.index, beta, binom);
+        if (j < 0) continue;
+        if constexpr (CPLX) {
+          const double2 xv = reinterpret_cast<const double2*>(x)[j * ldx + r];
+          are += c.x * xv.x - c.y * xv.y;
+          aim += c.x * xv.y + c.y * xv.x;
+        } else {
+          are += c.x * x[j * ldx + r];
+        }
+      }
+      if constexpr (CPLX) {
+        reinterpret_cast<double2*>(y)[row * ldy + r] = make_double2(are, aim);
+      } else {
+        y[row * ldy + r] = are;
+      }
+    }
+  }
+}
+
+}  // namespace lsg

@@ -1,0 +1,92 @@
+"""Lattices, symmetry generators and Hamiltonians of the standard workloads.
+
+These play the role of the reference's chapel/data/*.yaml configs: plain descriptions from which
+``Symmetries``, bases and ``Expr`` objects are built.
+"""
+
+from __future__ import annotations
+
+from typing import List, Sequence, Tuple
+
+from ._expr import Expr
+from ._group import Symmetries, Symmetry
+
+
+def chain_bonds(n: int) -> List[Tuple[int, int]]:
+    return [(i, (i + 1) % n) for i in range(n)]
+
+
+def chain_symmetries(n: int, momentum: int = 0, parity: int = None) -> List[Symmetry]:
+    gens = [Symmetry([(i + 1) % n for i in range(n)], momentum)]
+    if parity is not None:
+        gens.append(Symmetry(list(range(n))[::-1], parity))
+    return gens
+
+
+def square_index(x: int, y: int, L: int) -> int:
+    return (y % L) * L + (x % L)
+
+
+def square_bonds(L: int, diagonal: bool = False) -> List[Tuple[int, int]]:
+    """Nearest-neighbour (or next-nearest, diagonal=True) bonds of an L x L torus."""
+    out = []
+    for y in range(L):
+        for x in range(L):
+            i = square_index(x, y, L)
+            if not diagonal:
+                out.append((i, square_index(x + 1, y, L)))
+                out.append((i, square_index(x, y + 1, L)))
+            else:
+                out.append((i, square_index(x + 1, y + 1, L)))
+                out.append((i, square_index(x + 1, y - 1, L)))
+    return out
+
+
+def square_symmetries(L: int, kx: int = 0, ky: int = 0) -> List[Symmetry]:
+    """Translations (sectors kx, ky), the two reflections and the 90-degree rotation of an L x L
+    torus (the generator set of chapel/data/heisenberg_square_6x6.yaml)."""
+    tx = [square_index(i % L + 1, i // L, L) for i in range(L * L)]
+    ty = [square_index(i % L, i // L + 1, L) for i in range(L * L)]
+    rx = [square_index(L - 1 - i % L, i // L, L) for i in range(L * L)]
+    ry = [square_index(i % L, L - 1 - i // L, L) for i in range(L * L)]
+    rot = [square_index(L - 1 - i // L, i % L, L) for i in range(L * L)]
+    return [Symmetry(tx, kx), Symmetry(ty, ky), Symmetry(rx, 0), Symmetry(ry, 0), Symmetry(rot, 0)]
+
+
+def heisenberg(bonds: Sequence[Tuple[int, int]], J=1.0) -> Expr:
+    """J * sum (σˣσˣ + σʸσʸ + σᶻσᶻ) over bonds (the form of chapel/data/heisenberg_*.yaml)."""
+    e = Expr("σˣ₀ σˣ₁ + σʸ₀ σʸ₁ + σᶻ₀ σᶻ₁", sites=[list(b) for b in bonds])
+    return e.scale(J) if J != 1.0 else e
+
+
+def xxz(bonds, Jxy=1.0, delta=1.0) -> Expr:
+    exy = Expr("σˣ₀ σˣ₁ + σʸ₀ σʸ₁", sites=[list(b) for b in bonds]).scale(Jxy)
+    ez = Expr("σᶻ₀ σᶻ₁", sites=[list(b) for b in bonds]).scale(delta)
+    return exy + ez
+
+
+def dm_z(bonds, D=1.0) -> Expr:
+    """D * sum ẑ·(S_i × S_j) = D * sum (Sˣ_i Sʸ_j - Sʸ_i Sˣ_j) (imaginary σ⁺σ⁻ coefficients)."""
+    e = Expr("Sˣ₀ Sʸ₁ - Sʸ₀ Sˣ₁", sites=[list(b) for b in bonds])
+    return e.scale(D)
+
+
+def ladder(n_rungs: int):
+    """2-leg ladder, site (leg, r) -> leg * n_rungs + r; returns (leg bonds, rung bonds)."""
+    legs = [(l * n_rungs + r, l * n_rungs + (r + 1) % n_rungs) for l in (0, 1) for r in range(n_rungs)]
+    rungs = [(r, n_rungs + r) for r in range(n_rungs)]
+    return legs, rungs
+
+
+def ladder_symmetries(n_rungs: int, k: int = 0, exchange: int = 0) -> List[Symmetry]:
+    n = 2 * n_rungs
+    t = [(i // n_rungs) * n_rungs + (i % n_rungs + 1) % n_rungs for i in range(n)]
+    ex = [(i + n_rungs) % n for i in range(n)]
+    return [Symmetry(t, k), Symmetry(ex, exchange)]
+
+
+def hubbard(bonds, t=1.0, U=1.0, number_sites=None) -> Expr:
+    hop = Expr("c†₀↑ c₁↑ + c†₁↑ c₀↑ + c†₀↓ c₁↓ + c†₁↓ c₀↓", sites=[list(b) for b in bonds]).scale(-t)
+    n = number_sites if number_sites is not None else 1 + max(max(b) for b in bonds)
+    onsite = Expr("n₀↑ n₀↓", sites=[[i] for i in range(n)]).scale(U)
+    return hop + onsite
