@@ -1,0 +1,392 @@
+"""H*x throughput of the exact-diagonalization hot path on one GB300 (and N replicas).
+
+Workload (default, `--config j1j2_6x6`): J1-J2 Heisenberg model on the 6x6 square torus,
+J1 = 1, J2 = 0.5 (sigma.sigma form of chapel/data/heisenberg_square_6x6.yaml plus the diagonal
+bonds), Sz = 0, group = translations (36) x C4v (8) x spin inversion, momentum (pi, pi) sector,
+about 1.6e7 representatives, x complex128 with re/im ~ N(0, 1) from numpy seed 2.
+
+A step is one plain single-vector H*x (complex128) over the whole sector.
+
+    metric  = matrix elements / s = (D + NNZ) / t     (NNZ: off-diagonal elements of H)
+    value   = device-resident x, CUDA events around K steps on the launching stream
+    e2e     = the same metric through the reference-facing C-ABI call ls_chpl_matrix_vector_product
+              with host buffers (a complex x is two real calls), copies inside the timed region
+    extra   = block H*X with 16 right-hand sides and the adjoint H^dagger x, per vector
+
+`--impl reference` times the CPU restatement of the reference's algorithm (Benes orbit scan,
+scatter with atomics, prefix-table index; oracle/ls_oracle.c) with all host threads.
+"""
+
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+
+CONFIGS = {
+    "j1j2_6x6": dict(L=6, kx=3, ky=3, J2=0.5, inversion=1, seed=2,
+                     description="J1-J2 Heisenberg 6x6 torus, J2=0.5, Sz=0, T(36)xC4v(8)xZ2, (pi,pi) sector"),
+    "chain24": dict(chain=24, seed=1,
+                    description="Heisenberg chain N=24 PBC, Sz=0, T x P x Z2, k=0 p=+1 z=+1"),
+}
+
+
+# ------------------------------------------------------------------------------------------------
+def build_workload(ls, lat, name):
+    c = CONFIGS[name]
+    if "chain" in c:
+        n = c["chain"]
+        syms = ls.Symmetries(lat.chain_symmetries(n, 0, 0))
+        basis = ls.SpinBasis(n, n // 2, 1, syms)
+        expr = lat.heisenberg(lat.chain_bonds(n))
+    else:
+        L = c["L"]
+        syms = ls.Symmetries(lat.square_symmetries(L, c["kx"], c["ky"]))
+        basis = ls.SpinBasis(L * L, L * L // 2, c["inversion"], syms)
+        expr = lat.heisenberg(lat.square_bonds(L)) + lat.heisenberg(lat.square_bonds(L, diagonal=True), c["J2"])
+    return basis, expr
+
+
+def load_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.device_index = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device_index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_port_timing(basis, op, x, budget_s, threads):
+    """Times the oracle's reference-algorithm port on a bounded sample of columns.
+
+    Returns (elements_per_s, sample_description)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+
+    O.build()
+    O.set_threads(threads)
+    states = np.asarray(basis.states)
+    D = len(states)
+    if basis.has_permutation_symmetries:
+        gens = [(s.permutation, s.sector) for s in basis.symmetries.generators]
+        el = O.close_group(gens)
+        re, im = O.characters(el)
+        masks, shifts = basis.symmetries.network()
+        g = O.Group(np.array([e[0] for e in el]), re, im, basis._c.spin_inversion, basis.number_bits, masks, shifts)
+        projection = 2
+        import torch
+        norms = torch.as_tensor(basis.device_norms(), device="cuda").cpu().numpy() if D > 0 else np.ones(0)
+    else:
+        g, projection, norms = None, (1 if basis._c.spin_inversion else 0), np.ones(D)
+    off = O.Terms(*op._off_arrays)
+    diag = O.Terms(*op._diag_arrays)
+    xc = np.asarray(x)
+
+    def run(cols):
+        t0 = time.perf_counter()
+        _, st, nnz = O.matvec(g, projection, basis._c.spin_inversion, basis.number_bits, states, norms, off, diag,
+                              xc, complex_=np.iscomplexobj(xc), baseline=True, cols=(0, cols), return_nnz=True)
+        return time.perf_counter() - t0, nnz
+
+    n = min(D, 512)
+    t, _ = run(n)
+    while t < 1.0 and n < D:
+        n = min(D, n * 4)
+        t, _ = run(n)
+    per_col = t / n
+    cols = int(min(D, max(n, budget_s / max(per_col, 1e-12))))
+    t, nnz = run(cols)
+    # matrix elements processed by the sample: its diagonal entries plus the off-diagonal
+    # elements its columns generated
+    return cols, nnz, t
+
+
+# ------------------------------------------------------------------------------------------------
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement of the reference's algorithm on the host cores."""
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    ls = importlib.import_module("lattice-symmetries_gb300")
+    lat = importlib.import_module("lattice-symmetries_gb300.lattices")
+    basis, expr = build_workload(ls, lat, args.config)
+    op = ls.Operator(basis, expr)
+    gens = [(s.permutation, s.sector) for s in basis.symmetries.generators]
+    el = O.close_group(gens)
+    re, im = O.characters(el)
+    masks, shifts = basis.symmetries.network()
+    inv = basis._c.spin_inversion
+    g = O.Group(np.array([e[0] for e in el]), re, im, inv, basis.number_bits, masks, shifts)
+    lo, hi = basis._estimates()
+    t0 = time.perf_counter()
+    states = O.enumerate_projected(g, lo, hi, use_benes=True)
+    t_build = time.perf_counter() - t0
+    D = len(states)
+    norms = O.state_info(g, states, use_benes=True)[2]
+    rng = np.random.default_rng(CONFIGS[args.config]["seed"])
+    x = rng.normal(size=D) + 1j * rng.normal(size=D)
+    off = O.Terms(*op._off_arrays)
+    diag = O.Terms(*op._diag_arrays)
+    # calibrate columns per step for ~args.cpu_seconds / (steps + warmup) of work
+    per_step = max(1.0, args.cpu_seconds / max(1, args.steps + args.warmup))
+
+    def run(cols):
+        t = time.perf_counter()
+        _, _, nnz = O.matvec(g, 2, inv, basis.number_bits, states, norms, off, diag, x, complex_=True,
+                             baseline=True, cols=(0, cols), return_nnz=True)
+        return time.perf_counter() - t, nnz
+
+    n = min(D, 256)
+    t, _ = run(n)
+    while t < 0.5 and n < D:
+        n = min(D, n * 4)
+        t, _ = run(n)
+    cols = int(min(D, max(n, per_step / max(t / n, 1e-12))))
+    for _ in range(args.warmup):
+        run(cols)
+    runs = [run(cols) for _ in range(args.steps)]
+    tm = float(np.mean([r[0] for r in runs]))
+    nnz_sample = runs[0][1]
+    value = (cols + nnz_sample) / tm
+    line = {
+        "impl": "reference", "metric": "H*x matrix elements/s", "value": value, "unit": "elements/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": tm * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic", "config": {"workload": args.config, "number_states": D},
+        "cpu_baseline": {"value": value, "unit": "elements/s", "cores": threads, "kind": "port",
+                         "sample": "first {} of {} columns per step (scatter form), basis built on the host in {:.1f} s".format(
+                             cols, D, t_build)},
+        "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="j1j2_6x6", choices=sorted(CONFIGS))
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ls = importlib.import_module("lattice-symmetries_gb300")
+    lat = importlib.import_module("lattice-symmetries_gb300.lattices")
+    basis, expr = build_workload(ls, lat, args.config)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    basis.build()
+    t_build = time.perf_counter() - t0
+    op = ls.Operator(basis, expr)
+    D = basis.number_states
+    nnz = op.count_nonzeros()
+    elements = D + nnz
+    rng = np.random.default_rng(CONFIGS[args.config]["seed"])
+    x_host = rng.normal(size=D) + 1j * rng.normal(size=D)
+    x = torch.from_numpy(x_host).cuda()
+    y = torch.empty_like(x)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+
+    def step():
+        op.apply_device(x, out=y, stream=sptr, check=False)
+
+    for _ in range(args.warmup):
+        step()
+    op.check_errors(sptr)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        start.record(stream)
+        for _ in range(args.steps):
+            step()
+        end.record(stream)
+        torch.cuda.synchronize()
+    op.check_errors(sptr)
+    t_ms = start.elapsed_time(end)
+    if world > 1:
+        tt = torch.tensor([t_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    ms_per_step = t_ms / args.steps
+    value = world * elements * args.steps / (t_ms * 1e-3)
+
+    # roofline of the matvec kernel (one launch per step): algorithmic bytes
+    bytes_per_launch = 8 * D + 8 * D + 16 * D + 16 * D + nnz * (16 + 8 + 8)
+    achieved_gbs = bytes_per_launch / (ms_per_step * 1e-3) / 1e9
+    peak, peak_kind = load_peaks()
+
+    # block matvec (16 right-hand sides) and adjoint, per vector
+    extra = {}
+    K16 = 16
+    X16 = torch.from_numpy(rng.normal(size=(D, K16)) + 1j * rng.normal(size=(D, K16))).cuda()
+    Y16 = torch.empty_like(X16)
+    for _ in range(2):
+        op.apply_device(X16, out=Y16, stream=sptr, check=False)
+    torch.cuda.synchronize()
+    nb = max(1, args.steps // 2)
+    start.record(stream)
+    for _ in range(nb):
+        op.apply_device(X16, out=Y16, stream=sptr, check=False)
+    end.record(stream)
+    torch.cuda.synchronize()
+    t16 = start.elapsed_time(end) / nb
+    extra["block16"] = {"ms_per_block": t16, "value_per_vector": elements * K16 / (t16 * 1e-3),
+                        "speedup_per_vector_vs_plain": ms_per_step * K16 / t16}
+    for _ in range(2):
+        op.apply_device(x, out=y, adjoint=True, stream=sptr, check=False)
+    torch.cuda.synchronize()
+    start.record(stream)
+    for _ in range(nb):
+        op.apply_device(x, out=y, adjoint=True, stream=sptr, check=False)
+    end.record(stream)
+    torch.cuda.synchronize()
+    ta = start.elapsed_time(end) / nb
+    extra["adjoint"] = {"ms_per_step": ta, "value": elements / (ta * 1e-3)}
+    op.check_errors(sptr)
+
+    # end to end through the reference-facing C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        xr = np.ascontiguousarray(x_host.real)
+        xi = np.ascontiguousarray(x_host.imag)
+        op.apply_to_state_vector(xr)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ne = max(1, min(args.steps, 3))
+        for _ in range(ne):
+            yr = op.apply_to_state_vector(xr)
+            yi = op.apply_to_state_vector(xi)
+        te = (time.perf_counter() - t0) / ne
+        e2e = {"value": world * elements / te, "unit": "elements/s", "h2d_bytes_per_step": 2 * 8 * D,
+               "d2h_bytes_per_step": 2 * 8 * D, "path": "ls_chpl_matrix_vector_product x2 (real, imag)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        cols, nnz_cols, tc = cpu_port_timing(basis, op, x_host, args.cpu_seconds, threads)
+        cpu = {"value": (cols + nnz_cols) / tc, "unit": "elements/s", "cores": threads, "kind": "port",
+               "sample": "first {} of {} columns, scatter form (oracle/ls_oracle.c, Benes + atomics), {:.1f} s".format(
+                   cols, D, tc)}
+
+    if rank == 0:
+        line = {
+            "metric": "H*x matrix elements/s", "value": value, "unit": "elements/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": args.config, "description": CONFIGS[args.config]["description"],
+                       "number_states": D, "nnz": nnz, "rhs": 1, "parallelism": "replicas",
+                       "l2": "inputs larger than L2 (x 16 B/state, representatives + norms + index)"},
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",
+                         "frac": achieved_gbs / peak, "traffic": None, "peak_source": peak_kind,
+                         "note": "integer-pipe bound orbit scan; HBM fraction of algorithmic bytes"},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
+            "clocks": clocks.summary(), "basis_build_s": t_build, "extra": extra,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

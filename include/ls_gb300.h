@@ -252,8 +252,9 @@ void ls_chpl_matrix_vector_product(ls_hs_operator *matrix, int num_vectors, doub
  * 2. Additive symbols (no counterpart in the reference).
  *
  * All return 0 on success and a negative code on failure; ls_gpu_last_error() gives the message.
- * `stream` is a cudaStream_t (NULL = the library's stream).  Device pointers are CUDA global
- * memory on the current device.  Complex arrays are interleaved (re, im) float64 pairs.
+ * `stream` is a cudaStream_t; NULL is the legacy default stream, as everywhere in CUDA.  Device
+ * pointers are CUDA global memory on the current device.  Complex arrays are interleaved
+ * (re, im) float64 pairs, 16-byte aligned.
  * ------------------------------------------------------------------------------------------- */
 
 #define LS_GPU_OK 0
@@ -274,12 +275,20 @@ int ls_gpu_basis_info(ls_hs_basis const *basis, int64_t *number_states,
 
 /* y[D][k] = A x[D][k] for k right-hand sides stored row-major with leading dimension ld
  * (ld >= k), A = H (adjoint = 0) or A = H^dagger (adjoint = 1).  Complex128 x and y.
- * Full complex arithmetic: complex characters and coefficients are kept. */
+ * Full complex arithmetic: complex characters and coefficients are kept.
+ * Stream-ordered: returns after enqueueing (usable inside CUDA graph capture once the basis
+ * and operator data are resident); a generated state that leaves the basis is recorded on the
+ * device and reported by ls_gpu_check_errors. */
 int ls_gpu_matvec_c128(ls_hs_operator const *op, int k, double const *d_x, int64_t ldx,
                        double *d_y, int64_t ldy, int adjoint, void *stream);
 /* The same for real float64 vectors, with the reference's real-part semantics. */
 int ls_gpu_matvec_f64(ls_hs_operator const *op, int k, double const *d_x, int64_t ldx,
                       double *d_y, int64_t ldy, int adjoint, void *stream);
+/* Synchronises `stream`, returns LS_GPU_ERR_BASIS if a matvec since the last check generated a
+ * state outside its basis (and clears the flag), else 0. */
+int ls_gpu_check_errors(void *stream);
+/* Number of off-diagonal matrix elements (generated targets found in the basis) of H. */
+int ls_gpu_count_nonzeros(ls_hs_operator const *op, int64_t *nnz);
 
 /* Per-coupling inner products out[c] = <g, H_c x> for an operator whose terms are tagged with
  * coupling ids (term_coupling[t] in [0, n_couplings) for the off-diagonal terms, then the

@@ -7,7 +7,7 @@ reference's Haskell host layer: it closes the symmetry group, writes the Benes m
 non-branching term tables into the C structs of include/ls_gb300.h, and calls the C ABI of
 libls_gb300.so, whose kernels run on the GPU.
 
-Additions with no counterpart in the reference: ``Operator.matvec`` (device tensors, complex128,
+Additions with no counterpart in the reference: ``Operator.apply_device`` (device tensors, complex128,
 several right-hand sides, adjoint), ``Basis.device_states`` / ``device_norms``.
 """
 
@@ -27,6 +27,10 @@ try:  # scipy is optional for the LinearOperator base class
     from scipy.sparse.linalg import LinearOperator as _LinearOperator
 except Exception:  # pragma: no cover
     _LinearOperator = object
+try:  # array namespace that recent scipy versions expect on every LinearOperator
+    from scipy.sparse.linalg._interface import np_compat as _XP
+except Exception:  # pragma: no cover
+    _XP = np
 
 
 def _u64(x) -> np.ndarray:
@@ -38,7 +42,7 @@ class _DeviceArray:
 
     def __init__(self, ptr: int, shape, typestr: str, owner):
         self.__cuda_array_interface__ = {
-            "shape": tuple(shape), "typestr": typestr, "data": (int(ptr), True), "version": 3,
+            "shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False), "version": 3,
             "strides": None,
         }
         self._owner = owner
@@ -438,6 +442,10 @@ class Operator(_LinearOperator):
         self._c.off_diag_terms = ctypes.pointer(self._c_off) if self._c_off is not None else None
         self._c.diag_terms = ctypes.pointer(self._c_diag) if self._c_diag is not None else None
         self._lib = N.lib()
+        # LinearOperator state (dtype and shape are properties here, resolved once the basis is
+        # built, as in the reference's Operator)
+        self._xp = _XP
+        self.ndim = 2
 
     @property
     def _payload(self):
@@ -547,11 +555,12 @@ class Operator(_LinearOperator):
         return out
 
     # -- GPU (additive) ---------------------------------------------------------------------------
-    def matvec(self, x, out=None, adjoint: bool = False, stream=None):
+    def apply_device(self, x, out=None, adjoint: bool = False, stream=None, check: bool = True):
         """y = H x (or H^dagger x) on CUDA tensors: complex128 or float64, shape [D] or [D, k].
 
         Complex arithmetic is exact (complex characters and coefficients are kept); float64
-        follows the reference's real-part semantics.
+        follows the reference's real-part semantics.  With check=False the call is stream-ordered
+        and does not synchronise; errors are then reported by ``check_errors()``.
         """
         import torch
 
@@ -577,7 +586,21 @@ class Operator(_LinearOperator):
         f = self._lib.ls_gpu_matvec_c128 if X.dtype == torch.complex128 else self._lib.ls_gpu_matvec_f64
         rc = f(self._payload, k, X.data_ptr(), X.stride(0), Y.data_ptr(), Y.stride(0), int(adjoint), stream)
         N.check(rc, "matvec")
+        if check:
+            N.check(self._lib.ls_gpu_check_errors(stream), "matvec")
         return Y.reshape(D) if squeeze else Y
+
+    def check_errors(self, stream=None):
+        import torch
+        if stream is None:
+            stream = torch.cuda.current_stream().cuda_stream
+        N.check(self._lib.ls_gpu_check_errors(stream), "matvec")
+
+    def count_nonzeros(self) -> int:
+        """Off-diagonal matrix elements of H in this basis (generated targets found in the basis)."""
+        n = c_int64(0)
+        N.check(self._lib.ls_gpu_count_nonzeros(self._payload, byref(n)), "count_nonzeros")
+        return int(n.value)
 
 
 def load_library():

@@ -873,31 +873,33 @@ TermTable adjoint_terms(const TermTable& t) {
   return a;
 }
 
+// Device layout: v (double2, 16-byte aligned) first, then m, l, r, x, s (uint64).
 int upload_terms(const TermTable& t, DeviceTermSet* out) {
   const size_t n = (size_t)std::max(t.n, 1);
-  const size_t bytes = n * (5 * 8 + 16);
+  const size_t bytes = n * (16 + 5 * 8);
   std::vector<uint8_t> host(bytes, 0);
   uint8_t* p = host.data();
   auto put = [&](const void* src, size_t sz, size_t off) {
     if (t.n > 0) memcpy(p + off, src, sz);
   };
-  put(t.m.data(), t.n * 8, 0);
-  put(t.l.data(), t.n * 8, n * 8);
-  put(t.r.data(), t.n * 8, n * 16);
-  put(t.x.data(), t.n * 8, n * 24);
-  put(t.s.data(), t.n * 8, n * 32);
-  put(t.v.data(), t.n * 16, n * 40);
+  const size_t ov = 0, om = n * 16, ol = om + n * 8, orr = ol + n * 8, ox = orr + n * 8, os = ox + n * 8;
+  put(t.v.data(), t.n * 16, ov);
+  put(t.m.data(), t.n * 8, om);
+  put(t.l.data(), t.n * 8, ol);
+  put(t.r.data(), t.n * 8, orr);
+  put(t.x.data(), t.n * 8, ox);
+  put(t.s.data(), t.n * 8, os);
   if (!cuda_ok(cudaMalloc(&out->block, bytes), "cudaMalloc(terms)")) return LS_GPU_ERR_CUDA;
   if (!cuda_ok(cudaMemcpy(out->block, host.data(), bytes, cudaMemcpyHostToDevice), "upload terms"))
     return LS_GPU_ERR_CUDA;
   uint8_t* d = (uint8_t*)out->block;
   out->terms.n = t.n;
-  out->terms.m = (const uint64_t*)(d);
-  out->terms.l = (const uint64_t*)(d + n * 8);
-  out->terms.r = (const uint64_t*)(d + n * 16);
-  out->terms.x = (const uint64_t*)(d + n * 24);
-  out->terms.s = (const uint64_t*)(d + n * 32);
-  out->terms.v = (const double2*)(d + n * 40);
+  out->terms.v = (const double2*)(d + ov);
+  out->terms.m = (const uint64_t*)(d + om);
+  out->terms.l = (const uint64_t*)(d + ol);
+  out->terms.r = (const uint64_t*)(d + orr);
+  out->terms.x = (const uint64_t*)(d + ox);
+  out->terms.s = (const uint64_t*)(d + os);
   return 0;
 }
 
@@ -1058,17 +1060,60 @@ extern "C" int ls_gpu_basis_info(ls_hs_basis const* basis, int64_t* number_state
   return 0;
 }
 
+// Stream-ordered: enqueues the kernels and returns; a generated state outside the basis is
+// recorded in the device error word and reported by ls_gpu_check_errors.
 static int gpu_matvec(ls_hs_operator const* op, Scalar sc, int k, double const* d_x, int64_t ldx,
-                      double* d_y, int64_t ldy, int adjoint, void* stream) {
+                      double* d_y, int64_t ldy, int adjoint, void* stream,
+                      unsigned long long* nnz_counter = nullptr) {
   if (k < 0 || ldx < k || ldy < k) return fail(LS_GPU_ERR_INVALID, "invalid k / leading dimension");
   std::lock_guard<std::mutex> lock(g_mutex);
   MatvecProblem p;
   int rc = make_problem(op, adjoint != 0, &p);
   if (rc != 0) return rc;
-  cudaStream_t s = stream ? (cudaStream_t)stream : default_stream();
-  rc = launch_matvec(p, sc, k, d_x, ldx, d_y, ldy, device_error_word(), s);
-  if (rc != 0) return rc;
+  p.nnz_counter = nnz_counter;
+  cudaStream_t s = (cudaStream_t)stream;  // NULL: the legacy default stream (CUDA convention)
+  return launch_matvec(p, sc, k, d_x, ldx, d_y, ldy, device_error_word(), s);
+}
+
+extern "C" int ls_gpu_check_errors(void* stream) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  cudaStream_t s = (cudaStream_t)stream;  // NULL: the legacy default stream (CUDA convention)
   return read_and_clear_error(s);
+}
+
+extern "C" int ls_gpu_count_nonzeros(ls_hs_operator const* op, int64_t* nnz) {
+  int64_t n = 0;
+  {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    IndexData* ix = op && op->basis ? basis_index(op->basis) : nullptr;
+    if (ix == nullptr) return fail(LS_GPU_ERR_NOT_BUILT, "basis is not built on the GPU");
+    n = ix->n_states;
+  }
+  cudaStream_t s = default_stream();
+  double* d_x = nullptr;
+  double* d_y = nullptr;
+  unsigned long long* d_cnt = nullptr;
+  int rc = 0;
+  if (!cuda_ok(cudaMalloc((void**)&d_x, std::max<int64_t>(n, 1) * 8), "alloc") ||
+      !cuda_ok(cudaMalloc((void**)&d_y, std::max<int64_t>(n, 1) * 8), "alloc") ||
+      !cuda_ok(cudaMalloc((void**)&d_cnt, 8), "alloc")) {
+    rc = LS_GPU_ERR_CUDA;
+  }
+  if (rc == 0) {
+    cudaMemsetAsync(d_x, 0, std::max<int64_t>(n, 1) * 8, s);
+    cudaMemsetAsync(d_cnt, 0, 8, s);
+    rc = gpu_matvec(op, Scalar::Real, 1, d_x, 1, d_y, 1, 0, s, d_cnt);
+  }
+  unsigned long long h = 0;
+  if (rc == 0 && (!cuda_ok(cudaMemcpyAsync(&h, d_cnt, 8, cudaMemcpyDeviceToHost, s), "read nnz") ||
+                  !cuda_ok(cudaStreamSynchronize(s), "count")))
+    rc = LS_GPU_ERR_CUDA;
+  if (rc == 0) rc = ls_gpu_check_errors(s);
+  cudaFree(d_x);
+  cudaFree(d_y);
+  cudaFree(d_cnt);
+  if (rc == 0 && nnz) *nnz = (int64_t)h;
+  return rc;
 }
 
 extern "C" int ls_gpu_matvec_c128(ls_hs_operator const* op, int k, double const* d_x, int64_t ldx,
@@ -1086,7 +1131,7 @@ extern "C" int ls_gpu_state_info(ls_hs_basis const* basis, int64_t batch, uint64
   std::lock_guard<std::mutex> lock(g_mutex);
   const OrbitData* od = basis_orbit(basis);
   if (od == nullptr || od->n_elems == 0) return fail(LS_GPU_ERR_INVALID, "basis has no symmetry group on the GPU");
-  cudaStream_t s = stream ? (cudaStream_t)stream : default_stream();
+  cudaStream_t s = (cudaStream_t)stream;  // NULL: the legacy default stream (CUDA convention)
   const DeviceGroup* dg = orbit_device(od);
   if (dg == nullptr) return LS_GPU_ERR_CUDA;
   return launch_state_info(*dg, batch, d_alphas, d_betas, (double2*)d_characters, d_norms, 8, s);
@@ -1097,7 +1142,7 @@ extern "C" int ls_gpu_is_representative(ls_hs_basis const* basis, int64_t batch,
   std::lock_guard<std::mutex> lock(g_mutex);
   const OrbitData* od = basis_orbit(basis);
   if (od == nullptr || od->n_elems == 0) return fail(LS_GPU_ERR_INVALID, "basis has no symmetry group on the GPU");
-  cudaStream_t s = stream ? (cudaStream_t)stream : default_stream();
+  cudaStream_t s = (cudaStream_t)stream;  // NULL: the legacy default stream (CUDA convention)
   const DeviceGroup* dg = orbit_device(od);
   if (dg == nullptr) return LS_GPU_ERR_CUDA;
   return launch_is_representative(*dg, batch, d_alphas, d_flags, d_norms, 4, s);
@@ -1108,7 +1153,7 @@ extern "C" int ls_gpu_state_index(ls_hs_basis const* basis, int64_t batch, uint6
   std::lock_guard<std::mutex> lock(g_mutex);
   IndexData* ix = basis_index(basis);
   if (ix == nullptr) return fail(LS_GPU_ERR_NOT_BUILT, "basis is not built on the GPU");
-  cudaStream_t s = stream ? (cudaStream_t)stream : default_stream();
+  cudaStream_t s = (cudaStream_t)stream;  // NULL: the legacy default stream (CUDA convention)
   return launch_state_index(ix->dev, batch, d_alphas, d_indices, s);
 }
 

@@ -149,6 +149,7 @@ struct MatvecProblem {
   DeviceTerms off;           // terms applied to the row state through their l pattern
   DeviceTerms diag;
   int64_t n_rows;
+  unsigned long long* nnz_counter = nullptr;  // optional: counts off-diagonal elements found
 };
 
 int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, int64_t ldx,

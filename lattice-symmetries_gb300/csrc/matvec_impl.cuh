@@ -231,6 +231,7 @@ __global__ void __launch_bounds__(256, 2)
     if constexpr (CPLX) dim = warp_sum(dim);
 
     Acc acc;
+    unsigned found = 0;  // off-diagonal elements located by this lane (row total via warp sum)
     uint64_t my_rep = ~0ull;
     uint32_t my_idx = 0;
     double2 my_c = make_double2(0.0, 0.0);
@@ -242,6 +243,7 @@ __global__ void __launch_bounds__(256, 2)
       double fre = 0.0, fim = 0.0;
       if (lane < nslot) {
         j = mv_index_lookup(p.index, my_rep, binom);
+        found += (j >= 0);
         if (j >= 0) {
           double2 chi = S.chars[my_idx >> 1];
           if (INV && (my_idx & 1) && p.group.spin_inversion == -1) chi = make_double2(-chi.x, -chi.y);
@@ -321,6 +323,10 @@ __global__ void __launch_bounds__(256, 2)
       }
     }
     if (nslot > 0) flush();
+    if (p.nnz_counter != nullptr) {
+      const unsigned total = __reduce_add_sync(FULL, found);
+      if (lane == 0 && total) atomicAdd(p.nnz_counter, (unsigned long long)total);
+    }
 
     // reduce lanes holding the same right-hand side, add the diagonal, store
     if constexpr (CPLX) {
@@ -356,6 +362,7 @@ __global__ void __launch_bounds__(256)
   const Staged S = stage_problem(p, L, smem, false);
   const uint64_t flip = p.group.flip;
   const double chi_flip = (double)p.group.spin_inversion;
+  unsigned long long found = 0;
   for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < p.n_rows;
        row += (int64_t)gridDim.x * blockDim.x) {
     const uint64_t a = (p.index.identity) ? (uint64_t)row : __ldg(p.index.reps + row);
@@ -395,6 +402,7 @@ __global__ void __launch_bounds__(256)
         }
         const int64_t j = mv_index_lookup(p.index, beta, binom);
         if (j < 0) continue;
+        if (r == 0) ++found;
         if constexpr (CPLX) {
           const double2 xv = reinterpret_cast<const double2*>(x)[j * ldx + r];
           are += c.x * xv.x - c.y * xv.y;
@@ -410,6 +418,7 @@ __global__ void __launch_bounds__(256)
       }
     }
   }
+  if (p.nnz_counter != nullptr && found) atomicAdd(p.nnz_counter, found);
 }
 
 }  // namespace lsg

@@ -42,11 +42,15 @@ def square_bonds(L: int, diagonal: bool = False) -> List[Tuple[int, int]]:
     return out
 
 
-def square_symmetries(L: int, kx: int = 0, ky: int = 0) -> List[Symmetry]:
+def square_symmetries(L: int, kx: int = 0, ky: int = 0, point_group: bool = True) -> List[Symmetry]:
     """Translations (sectors kx, ky), the two reflections and the 90-degree rotation of an L x L
-    torus (the generator set of chapel/data/heisenberg_square_6x6.yaml)."""
+    torus (the generator set of chapel/data/heisenberg_square_6x6.yaml).  The point group is only
+    compatible with momenta it maps to themselves (e.g. 0 or (pi, pi)); point_group=False keeps
+    the translations only."""
     tx = [square_index(i % L + 1, i // L, L) for i in range(L * L)]
     ty = [square_index(i % L, i // L + 1, L) for i in range(L * L)]
+    if not point_group:
+        return [Symmetry(tx, kx), Symmetry(ty, ky)]
     rx = [square_index(L - 1 - i % L, i // L, L) for i in range(L * L)]
     ry = [square_index(i % L, L - 1 - i // L, L) for i in range(L * L)]
     rot = [square_index(L - 1 - i // L, i % L, L) for i in range(L * L)]

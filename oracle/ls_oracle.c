@@ -97,40 +97,62 @@ static inline void si_elem(const lso_group *g, si_acc *a, uint64_t x, uint64_t y
   }
 }
 
+static si_acc state_info_one(const lso_group *g, int W, int use_benes, uint64_t x) {
+  const int G = g->n_elems;
+  const int nchunks = G / W;
+  si_acc total = {x, 1.0, 0.0, 0.0};
+  si_acc lane;
+  for (int j = 0; j < W; ++j) {
+    lane.r = x; lane.cre = 1.0; lane.cim = 0.0; lane.n = 0.0;
+    for (int m = 0; m < nchunks; ++m) {
+      int e = m * W + j;
+      si_elem(g, &lane, x, image(g, e, x, use_benes), e);
+    }
+    if (j == 0) {
+      total = lane;
+    } else {
+      if (lane.r < total.r) {
+        total.r = lane.r;
+        total.cre = lane.cre;
+        total.cim = lane.cim;
+      }
+      total.n = total.n + lane.n;
+    }
+  }
+  for (int e = nchunks * W; e < G; ++e) si_elem(g, &total, x, image(g, e, x, use_benes), e);
+  return total;
+}
+
 void lso_state_info(const lso_group *g, int lane_width, int use_benes, int64_t count,
                     const uint64_t *xs, uint64_t *reps, double *chars /* 2*count */,
                     double *norms) {
   const int G = g->n_elems;
-  const int W = lane_width;
-  const int nchunks = G / W;
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < count; ++i) {
-    const uint64_t x = xs[i];
-    si_acc total = {x, 1.0, 0.0, 0.0};
-    si_acc lane;
-    for (int j = 0; j < W; ++j) {
-      lane.r = x; lane.cre = 1.0; lane.cim = 0.0; lane.n = 0.0;
-      for (int m = 0; m < nchunks; ++m) {
-        int e = m * W + j;
-        si_elem(g, &lane, x, image(g, e, x, use_benes), e);
-      }
-      if (j == 0) {
-        total = lane;
-      } else {
-        if (lane.r < total.r) {
-          total.r = lane.r;
-          total.cre = lane.cre;
-          total.cim = lane.cim;
-        }
-        total.n = total.n + lane.n;
-      }
-    }
-    for (int e = nchunks * W; e < G; ++e) si_elem(g, &total, x, image(g, e, x, use_benes), e);
+    si_acc total = state_info_one(g, lane_width, use_benes, xs[i]);
     reps[i] = total.r;
     chars[2 * i] = total.cre;
     chars[2 * i + 1] = total.cim;
     norms[i] = sqrt(total.n / (double)(g->spin_inversion == 0 ? G : 2 * G));
   }
+}
+
+/* Exact stabiliser sum: |Stab| when every stabiliser character has real part exactly 1, else 0. */
+static double exact_stabiliser_sum(const lso_group *g, int use_benes, uint64_t x) {
+  const uint64_t flip = flip_mask_of(g->n_bits);
+  int n = 0, trivial = 1;
+  for (int e = 0; e < g->n_elems; ++e) {
+    const uint64_t y = image(g, e, x, use_benes);
+    if (y == x) {
+      ++n;
+      if (g->chars_re[e] != 1.0) trivial = 0;
+    }
+    if (g->spin_inversion != 0 && (y ^ flip) == x) {
+      ++n;
+      if ((double)g->spin_inversion * g->chars_re[e] != 1.0) trivial = 0;
+    }
+  }
+  return trivial ? (double)n : 0.0;
 }
 
 /* ------------------------------------------------------------------------------------------ */
@@ -457,6 +479,7 @@ typedef struct {
 #define LSO_BENES 2       /* orbit scan through the Benes network (baseline) */
 #define LSO_PREFIX_INDEX 4 /* prefix-table index (baseline); else plain lower_bound */
 #define LSO_ATOMIC 8      /* OpenMP over columns with atomic adds (baseline); else serial */
+#define LSO_EXACT_NORMS 16 /* exact stabiliser sums for the generated states' norms */
 
 typedef struct {
   int projection;       /* 0 none, 1 inversion only, 2 full */
@@ -465,8 +488,9 @@ typedef struct {
   int state_index_identity;
 } lso_projection;
 
-/* Orbit scan with the reference's float order (W = 8 lanes) for the projected case. */
-static inline void project(const lso_group *g, const lso_projection *pr, int use_benes,
+/* Orbit scan with the reference's float order (W = 8 lanes) for the projected case; with
+ * exact_norms the norm uses the exact stabiliser sum instead of the floating sum of characters. */
+static inline void project(const lso_group *g, const lso_projection *pr, int use_benes, int exact_norms,
                            uint64_t beta, uint64_t *rep, double *cre, double *cim, double *norm) {
   if (pr->projection == 0) {
     *rep = beta; *cre = 1.0; *cim = 0.0; *norm = 1.0;
@@ -482,10 +506,12 @@ static inline void project(const lso_group *g, const lso_projection *pr, int use
     *norm = 1.0;
     return;
   }
-  double ch[2];
-  lso_state_info(g, 8, use_benes, 1, &beta, rep, ch, norm);
-  *cre = ch[0];
-  *cim = ch[1];
+  si_acc a = state_info_one(g, 8, use_benes, beta);
+  const double denom = (double)(g->spin_inversion == 0 ? g->n_elems : 2 * g->n_elems);
+  *rep = a.r;
+  *cre = a.cre;
+  *cim = a.cim;
+  *norm = sqrt((exact_norms ? exact_stabiliser_sum(g, use_benes, beta) : a.n) / denom);
 }
 
 /* y = H x over the representatives (BatchedOperator.chpl:139-282 + DistributedMatrixVector.chpl
@@ -493,9 +519,11 @@ static inline void project(const lso_group *g, const lso_projection *pr, int use
  * a state outside the basis (the reference halts there, DistributedMatrixVector.chpl:133). */
 int lso_matvec(const lso_group *g, const lso_projection *pr, int64_t D, const uint64_t *reps,
                const double *rep_norms, const lso_terms *off, const lso_terms *diag, int mode,
-               const double *x, double *y, int64_t row_begin, int64_t row_end) {
+               const double *x, double *y, int64_t row_begin, int64_t row_end, int64_t *nnz_out) {
+  int64_t nnz = 0;
   const int cplx = mode & LSO_COMPLEX;
   const int use_benes = (mode & LSO_BENES) != 0;
+  const int exact_norms = (mode & LSO_EXACT_NORMS) != 0;
   lso_index idx;
   int use_prefix = (mode & LSO_PREFIX_INDEX) != 0;
   if (use_prefix) lso_index_init(&idx, reps, D, pr->n_bits, 22);
@@ -527,7 +555,7 @@ int lso_matvec(const lso_group *g, const lso_projection *pr, int64_t D, const ui
     }
   }
   if (off != NULL && off->n > 0) {
-#pragma omp parallel for schedule(dynamic, 64) if (mode & LSO_ATOMIC)
+#pragma omp parallel for schedule(dynamic, 64) if (mode & LSO_ATOMIC) reduction(+ : nnz)
     for (int64_t j = row_begin; j < row_end; ++j) {
       const uint64_t a = reps[j];
       const double na = pr->projection == 2 ? rep_norms[j] : 1.0;
@@ -548,7 +576,7 @@ int lso_matvec(const lso_group *g, const lso_projection *pr, int64_t D, const ui
         const uint64_t beta = a ^ off->x[t];
         uint64_t rep;
         double chr, chi, nb;
-        project(g, pr, use_benes, beta, &rep, &chr, &chi, &nb);
+        project(g, pr, use_benes, exact_norms, beta, &rep, &chr, &chi, &nb);
         /* cs *= tempCoeffs * norms[k] / norms[alpha] (BatchedOperator.chpl:242-246) */
         double sr = cr * nb / na, si = ci * nb / na;
         double outr = chr * sr - chi * si, outi = chr * si + chi * sr;
@@ -567,6 +595,7 @@ int lso_matvec(const lso_group *g, const lso_projection *pr, int64_t D, const ui
           error = 1;
           continue;
         }
+        ++nnz;
         if (cplx) {
 #pragma omp atomic
           y[2 * i] += outr;
@@ -580,6 +609,7 @@ int lso_matvec(const lso_group *g, const lso_projection *pr, int64_t D, const ui
     }
   }
   if (use_prefix) lso_index_free(&idx);
+  if (nnz_out) *nnz_out = nnz;
   return error ? -1 : 0;
 }
 

@@ -53,7 +53,7 @@ class lso_projection(Structure):
                 ("state_index_identity", c_int)]
 
 
-LSO_COMPLEX, LSO_BENES, LSO_PREFIX_INDEX, LSO_ATOMIC = 1, 2, 4, 8
+LSO_COMPLEX, LSO_BENES, LSO_PREFIX_INDEX, LSO_ATOMIC, LSO_EXACT_NORMS = 1, 2, 4, 8, 16
 
 _lib = None
 
@@ -84,7 +84,7 @@ def lib():
         L.lso_matvec.restype = c_int
         L.lso_matvec.argtypes = [POINTER(lso_group), POINTER(lso_projection), c_int64, POINTER(c_uint64),
                                  POINTER(c_double), POINTER(lso_terms), POINTER(lso_terms), c_int,
-                                 POINTER(c_double), POINTER(c_double), c_int64, c_int64]
+                                 POINTER(c_double), POINTER(c_double), c_int64, c_int64, POINTER(c_int64)]
         L.lso_max_threads.restype = c_int
         L.lso_set_threads.argtypes = [c_int]
         _lib = L
@@ -209,8 +209,17 @@ class Terms:
 
 
 def matvec(g, projection, spin_inversion, n_bits, reps, rep_norms, off: Terms, diag: Terms, x,
-           complex_=False, baseline=False, cols=None, identity_index=False):
-    """y = H x by the reference's scatter algorithm (ls_oracle.c lso_matvec).  Returns (y, status)."""
+           complex_=False, baseline=False, cols=None, identity_index=False, return_nnz=False,
+           exact_norms=False):
+    """y = H x by the reference's scatter algorithm (ls_oracle.c lso_matvec).
+
+    exact_norms: norms of generated states from the exact stabiliser sum instead of the
+    reference's floating sum of characters (they differ only for orbits whose stabiliser
+    character is non-trivial in complex sectors, where the reference's sum is rounding noise
+    and its driver halts on the resulting index miss).
+
+    Returns (y, status), or (y, status, nnz) with return_nnz: the off-diagonal elements that the
+    processed columns contributed."""
     reps = np.ascontiguousarray(reps, dtype=np.uint64)
     D = reps.shape[0]
     if rep_norms is None:
@@ -228,15 +237,19 @@ def matvec(g, projection, spin_inversion, n_bits, reps, rep_norms, off: Terms, d
         xv = np.ascontiguousarray(x, dtype=np.float64)
         y = np.zeros(D, dtype=np.float64)
     mode = (LSO_COMPLEX if complex_ else 0) | ((LSO_BENES | LSO_PREFIX_INDEX | LSO_ATOMIC) if baseline else 0)
+    mode |= LSO_EXACT_NORMS if exact_norms else 0
     if g is None:
         g = Group(np.zeros((0, 1)), [], [], 0, n_bits)
     gc = ctypes.byref(g.c)
     c0, c1 = (-1, -1) if cols is None else cols
+    nnz = c_int64(0)
     st = lib().lso_matvec(gc, ctypes.byref(pr), D, _p(reps, c_uint64), _p(rep_norms, c_double),
                           ctypes.byref(off.c), ctypes.byref(diag.c), mode, _p(xv, c_double), _p(y, c_double),
-                          c0, c1)
+                          c0, c1, ctypes.byref(nnz))
     if complex_:
         y = y.view(np.complex128)
+    if return_nnz:
+        return y, st, int(nnz.value)
     return y, st
 
 

@@ -62,10 +62,19 @@ class Case:
             return O.state_info(self.group, reps)[2]
         return np.ones(len(reps))
 
-    def oracle_matvec(self, reps, x, complex_=False):
-        norms = self.oracle_norms(reps)
+    def oracle_norms_exact(self, reps):
+        if self.projection == 2:
+            _, cnt = O.orbit_exact(self.group, reps)
+            return np.sqrt(cnt / (self.group.order * (2 if self.inv else 1)))
+        return np.ones(len(reps))
+
+    def oracle_matvec(self, reps, x, complex_=False, exact_norms=True):
+        """The reference's scatter algorithm; by default with exact stabiliser norms (identical to
+        the reference's floating norms in real sectors)."""
+        norms = self.oracle_norms_exact(reps) if exact_norms else self.oracle_norms(reps)
         y, st = O.matvec(self.group, self.projection, self.inv, self.nbits, reps, norms, self.off, self.diag, x,
-                         complex_=complex_, identity_index=bool(self.basis._c.state_index_is_identity))
+                         complex_=complex_, identity_index=bool(self.basis._c.state_index_is_identity),
+                         exact_norms=exact_norms)
         assert st == 0
         return y
 
@@ -92,8 +101,8 @@ def config1_case(goldens):
     return Case(basis, expr, "config1")
 
 
-def square_case(L, kx=0, ky=0, inv=1, J2=0.0, h=None):
-    syms = ls.Symmetries(LAT.square_symmetries(L, kx, ky))
+def square_case(L, kx=0, ky=0, inv=1, J2=0.0, h=None, point_group=True):
+    syms = ls.Symmetries(LAT.square_symmetries(L, kx, ky, point_group))
     n = L * L
     basis = ls.SpinBasis(n, hamming_weight=h if h is not None else n // 2, spin_inversion=inv, symmetries=syms)
     expr = LAT.heisenberg(LAT.square_bonds(L))

@@ -190,6 +190,31 @@ def test_oracle_index_against_compiled_reference(ref_kernels):
     assert hasattr(L, "ls_hs_state_index_binary_search_kernel")
 
 
+@pytest.mark.parametrize("make", [lambda g: config1_case(g), lambda g: chain_case(16, k=8, p=1, inv=-1),
+                                  lambda g: square_case(4, 2, 2, inv=1, J2=0.5)])
+def test_exact_norms_equal_reference_norms_in_real_sectors(goldens, make):
+    """In real sectors the reference's floating stabiliser sums are exact, so the exact-norm
+    checker reproduces the reference's scatter bit for bit."""
+    case = make(goldens)
+    reps = case.oracle_states()
+    rng = np.random.default_rng(6)
+    x = rng.normal(size=len(reps))
+    y_ref = case.oracle_matvec(reps, x, exact_norms=False)
+    y_exact = case.oracle_matvec(reps, x, exact_norms=True)
+    assert np.array_equal(y_ref, y_exact)
+
+
+@pytest.mark.parametrize("n,k", [(14, 3), (13, 5), (16, 4), (20, 3)])
+def test_reference_rule_basis_has_no_noise_states(n, k):
+    """The reference keeps a state iff its floating stabiliser sum is > 0; in these complex
+    sectors that decision agrees with the exact one (no state with a non-trivial stabiliser
+    character survives), so the bit-exact basis is also the correct one."""
+    case = chain_case(n, k=k, h=n // 2)
+    reps = case.oracle_states()
+    _, cnt = O.orbit_exact(case.group, reps)
+    assert np.all(cnt > 0)
+
+
 def test_oracle_baseline_path_equals_checker():
     """The Benes/prefix-index/atomic baseline path computes the same H x as the checker path."""
     case = chain_case(16, k=0, p=0, inv=1)
