@@ -278,6 +278,7 @@ def main():
     D = basis.number_states
     nnz = op.count_nonzeros()
     elements = D + nnz
+    tuned = op.autotune(1)
     rng = np.random.default_rng(CONFIGS[args.config]["seed"])
     x_host = rng.normal(size=D) + 1j * rng.normal(size=D)
     x = torch.from_numpy(x_host).cuda()
@@ -381,6 +382,7 @@ def main():
                          "note": "integer-pipe bound orbit scan; HBM fraction of algorithmic bytes"},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
             "clocks": clocks.summary(), "basis_build_s": t_build, "extra": extra,
+            "autotune": {"threads": tuned[0], "waves": tuned[1], "ms": tuned[2]},
         }
         print(json.dumps(line))
     if world > 1:

@@ -314,8 +314,13 @@ int ls_gpu_is_representative(ls_hs_basis const *basis, int64_t batch, uint64_t c
 int ls_gpu_state_index(ls_hs_basis const *basis, int64_t batch, uint64_t const *d_alphas,
                        int64_t *d_indices, void *stream);
 
-/* Tuning knobs of the matvec kernels (rows per CTA, threads per CTA); 0 = automatic. */
-int ls_gpu_set_matvec_config(int threads_per_block, int blocks_per_sm);
+/* Tuning knobs of the projected matvec kernels: threads per CTA (256 or 320) and grid waves (the
+ * grid is 2 * SMs * waves CTAs, one warp per row at a time); 0 = default (256, 4). */
+int ls_gpu_set_matvec_config(int threads_per_block, int waves);
+/* Autotuner: times the matvec of `op` on k complex right-hand sides over a table of
+ * (threads, waves) pairs and installs the fastest; reports it and its time (ms). */
+int ls_gpu_autotune_matvec(ls_hs_operator const *op, int k, int *best_threads, int *best_waves,
+                           double *best_ms);
 
 #if defined(__cplusplus)
 } /* extern "C" */

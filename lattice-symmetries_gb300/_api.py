@@ -596,6 +596,14 @@ class Operator(_LinearOperator):
             stream = torch.cuda.current_stream().cuda_stream
         N.check(self._lib.ls_gpu_check_errors(stream), "matvec")
 
+    def autotune(self, k: int = 1):
+        """Times the GPU matvec over (threads per block, grid waves) and installs the fastest.
+        Returns (threads, waves, milliseconds)."""
+        th, wv, ms = ctypes.c_int(0), ctypes.c_int(0), c_double(0.0)
+        N.check(self._lib.ls_gpu_autotune_matvec(self._payload, int(k), byref(th), byref(wv), byref(ms)),
+                "autotune")
+        return th.value, wv.value, ms.value
+
     def count_nonzeros(self) -> int:
         """Off-diagonal matrix elements of H in this basis (generated targets found in the basis)."""
         n = c_int64(0)

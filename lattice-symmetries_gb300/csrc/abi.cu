@@ -434,8 +434,9 @@ extern "C" ls_hs_state_index_binary_search_data* ls_hs_create_state_index_binary
   }
   int shift = 0;
   int64_t range = 0;
+  uint64_t max_state = 0;
   if (build_prefix_index(ix->d_reps, ix->n_states, number_bits, ix->prefix_bits, &ix->d_offsets,
-                         &range, &shift, s) != 0 ||
+                         &range, &shift, s, &max_state) != 0 ||
       !cuda_ok(cudaStreamSynchronize(s), "build index")) {
     report("ls_hs_create_state_index_binary_search_kernel_data");
     cudaFree(ix->d_reps);
@@ -448,6 +449,7 @@ extern "C" ls_hs_state_index_binary_search_data* ls_hs_create_state_index_binary
   ix->dev.shift = shift;
   ix->dev.range_size = range;
   ix->dev.prefix_bits = ix->prefix_bits;
+  ix->dev.max_state = max_state;
   return ix;
 }
 
@@ -873,22 +875,46 @@ TermTable adjoint_terms(const TermTable& t) {
   return a;
 }
 
-// Device layout: v (double2, 16-byte aligned) first, then m, l, r, x, s (uint64).
-int upload_terms(const TermTable& t, DeviceTermSet* out) {
+// Whether applying a term can change a particle number that the basis conserves.
+bool term_breaks_constraint(const DeviceConstraint& c, uint64_t l, uint64_t r) {
+  if (c.kind == 0) return false;
+  if (c.kind == 1) return __builtin_popcountll(l) != __builtin_popcountll(r);
+  const uint64_t lo = c.half_bits >= 64 ? ~0ull : ((1ull << c.half_bits) - 1);
+  return __builtin_popcountll(l & lo) != __builtin_popcountll(r & lo) ||
+         __builtin_popcountll(l & ~lo) != __builtin_popcountll(r & ~lo);
+}
+
+// Device layout: v (double2, 16-byte aligned) first, then m, l, r, x, s (uint64), xinfo (uint32).
+int upload_terms(const TermTable& t, const DeviceConstraint& cons, DeviceTermSet* out) {
   const size_t n = (size_t)std::max(t.n, 1);
-  const size_t bytes = n * (16 + 5 * 8);
+  const size_t bytes = n * (16 + 5 * 8 + 4);
   std::vector<uint8_t> host(bytes, 0);
   uint8_t* p = host.data();
   auto put = [&](const void* src, size_t sz, size_t off) {
     if (t.n > 0) memcpy(p + off, src, sz);
   };
   const size_t ov = 0, om = n * 16, ol = om + n * 8, orr = ol + n * 8, ox = orr + n * 8, os = ox + n * 8;
+  const size_t oi = os + n * 8;
   put(t.v.data(), t.n * 16, ov);
   put(t.m.data(), t.n * 8, om);
   put(t.l.data(), t.n * 8, ol);
   put(t.r.data(), t.n * 8, orr);
   put(t.x.data(), t.n * 8, ox);
   put(t.s.data(), t.n * 8, os);
+  std::vector<uint32_t> xinfo(n, 0);
+  int all_two = t.n > 0 ? 1 : 0;
+  for (int k = 0; k < t.n; ++k) {
+    const uint64_t x = t.x[k];
+    const int cnt = __builtin_popcountll(x);
+    const int lo = x ? __builtin_ctzll(x) : 0;
+    const int hi = x ? 63 - __builtin_clzll(x) : 0;
+    uint32_t info = (uint32_t)lo | ((uint32_t)hi << 8) | ((uint32_t)cnt << 16);
+    if (term_breaks_constraint(cons, t.l[k], t.r[k])) info |= kTermNeedsCheck;
+    xinfo[k] = info;
+    if (cnt != 2) all_two = 0;
+  }
+  put(xinfo.data(), t.n * 4, oi);
+  out->terms.all_two_site = all_two;
   if (!cuda_ok(cudaMalloc(&out->block, bytes), "cudaMalloc(terms)")) return LS_GPU_ERR_CUDA;
   if (!cuda_ok(cudaMemcpy(out->block, host.data(), bytes, cudaMemcpyHostToDevice), "upload terms"))
     return LS_GPU_ERR_CUDA;
@@ -900,6 +926,7 @@ int upload_terms(const TermTable& t, DeviceTermSet* out) {
   out->terms.r = (const uint64_t*)(d + orr);
   out->terms.x = (const uint64_t*)(d + ox);
   out->terms.s = (const uint64_t*)(d + os);
+  out->terms.xinfo = (const uint32_t*)(d + oi);
   return 0;
 }
 
@@ -921,8 +948,9 @@ OperatorCache* operator_cache(const ls_hs_operator* op) {
   OperatorCache* c = new OperatorCache();
   c->off = read_terms(op->off_diag_terms);
   c->diag = read_terms(op->diag_terms);
-  if (upload_terms(c->off, &c->fwd_off) || upload_terms(adjoint_terms(c->off), &c->adj_off) ||
-      upload_terms(c->diag, &c->fwd_diag) || upload_terms(adjoint_terms(c->diag), &c->adj_diag)) {
+  const DeviceConstraint cons = op->basis ? basis_constraint(op->basis) : DeviceConstraint{};
+  if (upload_terms(c->off, cons, &c->fwd_off) || upload_terms(adjoint_terms(c->off), cons, &c->adj_off) ||
+      upload_terms(c->diag, cons, &c->fwd_diag) || upload_terms(adjoint_terms(c->diag), cons, &c->adj_diag)) {
     free_cache(c);
     return nullptr;
   }
@@ -1073,6 +1101,67 @@ static int gpu_matvec(ls_hs_operator const* op, Scalar sc, int k, double const* 
   p.nnz_counter = nnz_counter;
   cudaStream_t s = (cudaStream_t)stream;  // NULL: the legacy default stream (CUDA convention)
   return launch_matvec(p, sc, k, d_x, ldx, d_y, ldy, device_error_word(), s);
+}
+
+extern "C" int ls_gpu_check_errors(void* stream);
+
+// Times the matvec of `op` on k complex right-hand sides for every (threads per block, grid
+// waves) pair of a small table and installs the fastest with ls_gpu_set_matvec_config.
+extern "C" int ls_gpu_autotune_matvec(ls_hs_operator const* op, int k, int* best_threads, int* best_waves,
+                                      double* best_ms) {
+  if (k < 1) return fail(LS_GPU_ERR_INVALID, "k must be positive");
+  int64_t n = 0;
+  {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    IndexData* ix = op && op->basis ? basis_index(op->basis) : nullptr;
+    if (ix == nullptr) return fail(LS_GPU_ERR_NOT_BUILT, "basis is not built on the GPU");
+    n = ix->n_states;
+  }
+  cudaStream_t s = default_stream();
+  double* d_x = nullptr;
+  double* d_y = nullptr;
+  const size_t bytes = (size_t)std::max<int64_t>(n, 1) * k * 16;
+  if (!cuda_ok(cudaMalloc((void**)&d_x, bytes), "alloc") || !cuda_ok(cudaMalloc((void**)&d_y, bytes), "alloc")) {
+    cudaFree(d_x);
+    return LS_GPU_ERR_CUDA;
+  }
+  cudaMemsetAsync(d_x, 0, bytes, s);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int threads_choices[] = {256, 320};
+  const int wave_choices[] = {1, 2, 4, 8};
+  double best = 1e300;
+  int bt = 256, bw = 2, rc = 0;
+  for (int th : threads_choices) {
+    for (int wv : wave_choices) {
+      set_matvec_config(th, wv);
+      rc = gpu_matvec(op, Scalar::Complex, k, d_x, k, d_y, k, 0, s);  // warm-up / validation
+      if (rc != 0) break;
+      cudaEventRecord(e0, s);
+      rc = gpu_matvec(op, Scalar::Complex, k, d_x, k, d_y, k, 0, s);
+      cudaEventRecord(e1, s);
+      if (rc != 0 || !cuda_ok(cudaEventSynchronize(e1), "autotune")) break;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) {
+        best = ms;
+        bt = th;
+        bw = wv;
+      }
+    }
+    if (rc != 0) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d_x);
+  cudaFree(d_y);
+  if (rc == 0) rc = ls_gpu_check_errors(s);
+  set_matvec_config(bt, bw);
+  if (best_threads) *best_threads = bt;
+  if (best_waves) *best_waves = bw;
+  if (best_ms) *best_ms = best;
+  return rc;
 }
 
 extern "C" int ls_gpu_check_errors(void* stream) {

@@ -452,14 +452,34 @@ int compute_site_images(OrbitData* od) {
   std::vector<double2> chars(G);
   for (int e = 0; e < G; ++e) chars[e] = make_double2(od->chars_re[e], od->chars_im[e]);
 
-  // One block: masks_t | shifts | chars | onehot | prio (16-byte aligned pieces).
+  // Packed tables of the matvec kernels (see DeviceGroup::onehot_packed).  Available when the
+  // bits below the shifted state can hold the candidate index 2 * slot + flip.
+  int gpl = G > 0 ? pick_gpl_for(G) : -1;
+  if (gpl > 0) {
+    const int idx_bits = 32 - __builtin_clz((unsigned)(2 * 32 * gpl - 1));
+    if (B < 1 || 64 - B < idx_bits) gpl = -1;
+  }
+  const int Gp = gpl > 0 ? 32 * gpl : 0;
+  std::vector<uint64_t> onehot_packed((size_t)B * Gp);
+  std::vector<double2> chars_packed(Gp);
+  for (int s = 0; s < Gp; ++s) {
+    const int e = s < G ? s : 0;
+    chars_packed[s] = chars[e];
+    for (int b = 0; b < B; ++b) onehot_packed[(size_t)b * Gp + s] = onehot[(size_t)b * G + e] << (64 - B);
+  }
+  od->gpl = gpl > 0 ? gpl : 0;
+
+  // One block: masks_t | shifts | chars | onehot | prio | onehot_packed | chars_packed
+  // (16-byte aligned pieces).
   auto align16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
   od->off_masks = 0;
   od->off_shifts = align16(od->off_masks + masks_t.size() * 8);
   od->off_chars = align16(od->off_shifts + (size_t)std::max(D, 1) * 4);
   od->off_onehot = align16(od->off_chars + (size_t)std::max(G, 1) * 16);
   od->off_prio = align16(od->off_onehot + std::max<size_t>(onehot.size(), 1) * 8);
-  const size_t total = align16(od->off_prio + (size_t)std::max(G, 1) * 2) + 16;
+  od->off_onehot_packed = align16(od->off_prio + (size_t)std::max(G, 1) * 2);
+  od->off_chars_packed = align16(od->off_onehot_packed + std::max<size_t>(onehot_packed.size(), 1) * 8);
+  const size_t total = align16(od->off_chars_packed + (size_t)std::max(Gp, 1) * 16) + 16;
   od->host_block.assign(total, 0);
   uint8_t* h = od->host_block.data();
   if (!masks_t.empty()) memcpy(h + od->off_masks, masks_t.data(), masks_t.size() * 8);
@@ -467,6 +487,9 @@ int compute_site_images(OrbitData* od) {
   if (G > 0) memcpy(h + od->off_chars, chars.data(), (size_t)G * 16);
   if (!onehot.empty()) memcpy(h + od->off_onehot, onehot.data(), onehot.size() * 8);
   if (G > 0) memcpy(h + od->off_prio, prio.data(), (size_t)G * 2);
+  if (!onehot_packed.empty())
+    memcpy(h + od->off_onehot_packed, onehot_packed.data(), onehot_packed.size() * 8);
+  if (Gp > 0) memcpy(h + od->off_chars_packed, chars_packed.data(), (size_t)Gp * 16);
   DeviceGroup probe;
   od->standard_shifts = standard_shifts(probe, od->shifts);
   return 0;
@@ -500,6 +523,9 @@ const DeviceGroup* orbit_device(const OrbitData* od) {
   g.chars = (const double2*)(base + od->off_chars);
   g.onehot = (const uint64_t*)(base + od->off_onehot);
   g.prio = (const uint16_t*)(base + od->off_prio);
+  g.gpl = od->gpl;
+  g.onehot_packed = od->gpl > 0 ? (const uint64_t*)(base + od->off_onehot_packed) : nullptr;
+  g.chars_packed = od->gpl > 0 ? (const double2*)(base + od->off_chars_packed) : nullptr;
   od->dev_block = d;
   od->dev_device = dev;
   return &od->dev;
@@ -926,11 +952,25 @@ __global__ void k_bucket_clamp(int64_t* __restrict__ offsets, int64_t n_buckets,
   }
 }
 
+// The reference buckets on the top prefix_bits of number_bits (indexing.c:94-117).  Sorted
+// representatives are orbit minima and crowd towards small values, so here the buckets cover the
+// bits actually used (up to the largest representative) and their count grows with the basis
+// (about two states per bucket, at most 2^26 buckets); the answers are the same indices.
 int build_prefix_index(const uint64_t* d_reps, int64_t n, int number_bits, int prefix_bits,
-                       int64_t** d_offsets, int64_t* range_size, int* shift, cudaStream_t s) {
-  int p = std::min(prefix_bits, number_bits);
+                       int64_t** d_offsets, int64_t* range_size, int* shift, cudaStream_t s,
+                       uint64_t* max_state) {
+  uint64_t max_rep = 0;
+  if (n > 0 && !cuda_ok(cudaMemcpyAsync(&max_rep, d_reps + (n - 1), 8, cudaMemcpyDeviceToHost, s), "read max") )
+    return LS_GPU_ERR_CUDA;
+  if (!cuda_ok(cudaStreamSynchronize(s), "read max")) return LS_GPU_ERR_CUDA;
+  *max_state = n > 0 ? max_rep : 0;
+  const int used_bits = max_rep == 0 ? 1 : 64 - __builtin_clzll(max_rep);
+  int want = 1;
+  while (want < 26 && ((int64_t)1 << want) < n) ++want;
+  int p = std::max(std::min(prefix_bits, number_bits), want);
+  p = std::min(p, std::min(used_bits, 26));
   if (p < 0) p = 0;
-  *shift = number_bits - p;
+  *shift = used_bits - p;
   const int64_t nb = (int64_t)1 << p;
   int64_t* off = nullptr;
   unsigned long long* mx = nullptr;
@@ -965,7 +1005,7 @@ __device__ __forceinline__ int64_t index_lookup(const DeviceIndex& ix, uint64_t 
   if (ix.identity) return (int64_t)needle;
   if (ix.combinadic) return d_rank(needle) - ix.rank_base;
   int64_t len = ix.range_size;
-  if (len <= 0) return -1;
+  if (len <= 0 || needle > ix.max_state) return -1;
   int64_t base = __ldg(ix.offsets + (needle >> ix.shift));
   while (len > 1) {
     const int64_t half = len >> 1;

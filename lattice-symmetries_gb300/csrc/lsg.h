@@ -28,7 +28,22 @@ struct DeviceGroup {
   const double2* chars = nullptr;     // [n_elems] characters
   const uint64_t* onehot = nullptr;   // [n_bits][n_elems]: image of the one-bit state 1<<b under g
   const uint16_t* prio = nullptr;     // [n_elems] tie-break priority of state_info (lane order)
+  // Packed tables of the matvec kernels: the group padded to gpl * 32 slots (slot s holds element
+  // s, or element 0 for s >= n_elems), images shifted to the top bits (<< (64 - n_bits)) so that
+  // the low bits can carry the candidate index 2 * slot + flip.
+  int gpl = 0;                              // slots per lane (0: packed tables unavailable)
+  const uint64_t* onehot_packed = nullptr;  // [n_bits][gpl * 32]
+  const double2* chars_packed = nullptr;    // [gpl * 32]
 };
+
+// Slots per lane of the matvec kernels for a group of n elements (ascending choices).
+constexpr int kGplSet[] = {1, 2, 3, 4, 6, 9, 12, 16};
+inline int pick_gpl_for(int n_elems) {
+  const int need = (n_elems + 31) / 32;
+  for (int g : kGplSet)
+    if (g >= need) return g;
+  return -1;
+}
 
 // Device view of a sorted representative array and its prefix-bucket index.
 struct DeviceIndex {
@@ -39,6 +54,7 @@ struct DeviceIndex {
   int shift = 0;                      // bucket = state >> shift
   int64_t range_size = 0;             // window length
   int prefix_bits = 0;
+  uint64_t max_state = ~0ull;         // largest representative (larger needles are absent)
   int identity = 0;                   // index(state) = state
   // combinadics ranking (fixed Hamming weight, no projection): index = rank(state) - rank_base
   int combinadic = 0;
@@ -62,7 +78,12 @@ struct DeviceTerms {
   const uint64_t* s = nullptr;
   const double2* v = nullptr;
   const int32_t* coupling = nullptr;  // optional coupling id per term
+  // Per term: bits 0-7 lowest flipped site, 8-15 highest flipped site, 16-23 number of flipped
+  // sites, bit 24 set when the term can change a conserved particle number of the basis.
+  const uint32_t* xinfo = nullptr;
+  int all_two_site = 0;               // every term flips exactly two sites
 };
+constexpr uint32_t kTermNeedsCheck = 1u << 24;
 
 // Host-side records behind the opaque kernel-data pointers of the plugin tables.
 struct OrbitData {
@@ -75,6 +96,8 @@ struct OrbitData {
   // uploaded on first use so that kernel data can be created on a machine without a GPU.
   std::vector<uint8_t> host_block;
   size_t off_masks = 0, off_shifts = 0, off_chars = 0, off_onehot = 0, off_prio = 0;
+  size_t off_onehot_packed = 0, off_chars_packed = 0;
+  int gpl = 0;  // packed tables present when > 0
   bool standard_shifts = true;
   mutable DeviceGroup dev;
   mutable void* dev_block = nullptr;  // one allocation holding all device arrays
@@ -130,7 +153,8 @@ int enumerate_states(const DeviceGroup* g, const EnumerateRequest& req, uint64_t
                      int64_t* count, cudaStream_t s);
 
 int build_prefix_index(const uint64_t* d_reps, int64_t n, int number_bits, int prefix_bits,
-                       int64_t** d_offsets, int64_t* range_size, int* shift, cudaStream_t s);
+                       int64_t** d_offsets, int64_t* range_size, int* shift, cudaStream_t s,
+                       uint64_t* max_state);
 int launch_state_index(const DeviceIndex& ix, int64_t n, const uint64_t* d_x, int64_t* d_out,
                        cudaStream_t s);
 

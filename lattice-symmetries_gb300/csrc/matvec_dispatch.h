@@ -4,20 +4,37 @@
 
 namespace lsg {
 struct SmemLayout;
+struct PackedLayout;
 struct LaunchShape {
   int blocks;
   int threads;
 };
-// Returns 0 on success, LS_GPU_ERR_INVALID when no instantiation matches.
+// All return 0 on success, LS_GPU_ERR_INVALID when no instantiation matches.
+
+// Fallback projected kernel (no packing), one right-hand side.
 int launch_projected_real(int gpl, bool inv, const MatvecProblem& p, const SmemLayout& L,
                           LaunchShape sh, const double* x, int64_t ldx, double* y, int64_t ldy,
                           int* err, const uint64_t* binom, cudaStream_t s);
-int launch_projected_cplx(int gpl, bool inv, int k, const MatvecProblem& p, const SmemLayout& L,
-                          LaunchShape sh, const double* x, int64_t ldx, double* y, int64_t ldy,
-                          int* err, const uint64_t* binom, cudaStream_t s);
+int launch_projected_cplx_k1(int gpl, bool inv, const MatvecProblem& p, const SmemLayout& L,
+                             LaunchShape sh, const double* x, int64_t ldx, double* y, int64_t ldy,
+                             int* err, const uint64_t* binom, cudaStream_t s);
+
+// Packed projected kernel: real (k = 1) or complex (k in {1, 4, 8, 16}).
+int launch_packed(bool cplx, int k, int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L,
+                  LaunchShape sh, const double* x, int64_t ldx, double* y, int64_t ldy, int* err,
+                  const uint64_t* binom, cudaStream_t s);
+#define LSG_DECLARE_PACKED(NAME)                                                                  \
+  int NAME(int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L, LaunchShape sh,      \
+           const double* x, int64_t ldx, double* y, int64_t ldy, int* err, const uint64_t* binom, \
+           cudaStream_t s);
+LSG_DECLARE_PACKED(launch_packed_real)
+LSG_DECLARE_PACKED(launch_packed_cplx_k1)
+LSG_DECLARE_PACKED(launch_packed_cplx_k4)
+LSG_DECLARE_PACKED(launch_packed_cplx_k8)
+LSG_DECLARE_PACKED(launch_packed_cplx_k16)
+
+// Unprojected / spin-inversion-only kernel.
 int launch_plain(bool cplx, bool inv, int k, const MatvecProblem& p, const SmemLayout& L,
                  LaunchShape sh, const double* x, int64_t ldx, double* y, int64_t ldy, int* err,
                  const uint64_t* binom, cudaStream_t s);
-// group elements per lane supported by the projected kernels (ascending)
-constexpr int kGplChoices[] = {1, 2, 3, 4, 6, 9, 12, 16};
 }  // namespace lsg
