@@ -314,6 +314,24 @@ int ls_gpu_is_representative(ls_hs_basis const *basis, int64_t batch, uint64_t c
 int ls_gpu_state_index(ls_hs_basis const *basis, int64_t batch, uint64_t const *d_alphas,
                        int64_t *d_indices, void *stream);
 
+/* Basis enumeration that allocates nothing.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory: code running under a framework that owns every
+ * device allocation (its pool reserves the GPU's memory and hands out buffers), or code between
+ * stream captures, where cudaMalloc must not be called.  Writes the sorted representatives of
+ * `basis` -- the same array ls_hs_build_representatives produces -- into the caller's device
+ * buffer d_out of `capacity` entries and stores their number in *count (host memory).
+ *
+ * All scratch (the group tables, per-tile counts and offsets, scan sums) lives in one file-scope
+ * device array of 16 MiB that every GPU loading the library holds until the process exits.  The
+ * first call on a device looks up that array's device address (cudaGetSymbolAddress); make the
+ * first call before any stream capture.  Limits: group tables up to 1 MiB and about 5.2e9
+ * candidate states (LS_GPU_ERR_INVALID beyond, with a message); LS_GPU_ERR_INVALID also when
+ * *count exceeds `capacity` (nothing is written past d_out[capacity - 1]).  Calls share the
+ * array, so calls that overlap on the GPU race; the call synchronises `stream` before returning. */
+int ls_gpu_enumerate_noalloc(ls_hs_basis const *basis, uint64_t *d_out, int64_t capacity,
+                             int64_t *count, void *stream);
+
 /* Tuning knobs of the projected matvec kernels: threads per CTA (256 or 320) and grid waves (the
  * grid is 2 * SMs * waves CTAs, one warp per row at a time); 0 = default (256, 4). */
 int ls_gpu_set_matvec_config(int threads_per_block, int waves);

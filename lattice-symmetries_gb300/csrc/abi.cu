@@ -646,6 +646,43 @@ static int enumerate_into(ls_hs_basis const* b, uint64_t** d_out, int64_t* count
   return enumerate_states(g, req, d_out, count, default_stream());
 }
 
+// Allocation-free enumeration for callers that cannot allocate device memory; see
+// include/ls_gb300.h and the scratch description in basis.cu.  It builds the same request as
+// enumerate_into but never uploads the group through cudaMalloc: the group tables are copied into
+// the static scratch on every call.
+extern "C" int ls_gpu_enumerate_noalloc(ls_hs_basis const* b, uint64_t* d_out, int64_t capacity,
+                                        int64_t* count, void* stream) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (b == nullptr || count == nullptr) return fail(LS_GPU_ERR_INVALID, "basis and count must not be NULL");
+  if (basis_number_bits(b) > 64) return fail(LS_GPU_ERR_INVALID, "bases with more than 64 bits are not supported");
+  EnumerateRequest req{};
+  uint64_t lo, hi;
+  state_estimates(b, &lo, &hi);
+  req.lower = lo;
+  req.upper = hi;
+  req.number_sites = b->number_sites;
+  req.spin_inversion = b->spin_inversion;
+  req.hamming_fixed = hamming_fixed(b);
+  req.reference_norm_rule = 1;
+  const OrbitData* od = nullptr;
+  if (b->particle_type == LS_HS_SPIN) {
+    if (has_permutations(b)) {
+      req.mode = 0;
+      od = basis_orbit(b);
+    } else {
+      req.mode = 1;
+    }
+  } else if (b->particle_type == LS_HS_SPINFUL_FERMION) {
+    req.mode = b->number_up >= 0 ? 2 : 1;
+    req.spin_inversion = 0;
+  } else {
+    req.mode = 1;
+    req.spin_inversion = 0;
+  }
+  if (req.mode == 1 && b->particle_type == LS_HS_SPINFUL_FERMION) req.number_sites = 2 * b->number_sites;
+  return enumerate_states_noalloc(od, req, d_out, capacity, count, (cudaStream_t)stream);
+}
+
 extern "C" void ls_chpl_enumerate_representatives(ls_hs_basis* p, uint64_t lower, uint64_t upper,
                                                   chpl_external_array* dest) {
   (void)lower;  // the reference derives the range from the basis (StatesEnumeration.chpl:683-689)

@@ -1032,4 +1032,236 @@ int launch_state_index(const DeviceIndex& ix, int64_t n, const uint64_t* d_x, in
   return cuda_ok(cudaGetLastError(), "k_state_index") ? 0 : LS_GPU_ERR_CUDA;
 }
 
+// ================================================================================================
+// Allocation-free enumeration (ls_gpu_enumerate_noalloc).
+//
+// Some callers cannot allocate device memory: code that runs under a framework owning every
+// device allocation (a custom call of an array framework, a pool that reserves all of HBM), or
+// code between stream captures where cudaMalloc must not be called.  For them the enumeration runs
+// in two passes (count per tile, then write straight into the caller's output at scanned offsets)
+// and keeps all of its scratch in g_noalloc_scratch, a file-scope device array of
+// kNoallocScratchBytes that every GPU loading the library holds until the process exits:
+//   [0, kNoallocGroupBytes)   the basis' group tables, copied from the host on every call
+//   [kNoallocGroupBytes, ..)  tile counts (int32), tile offsets (int64), scan block sums (int64)
+// Each call overwrites everything it reads, so nothing needs clearing between calls; calls that
+// overlap on the GPU (different streams, or another host thread) race on the array.
+// ================================================================================================
+constexpr size_t kNoallocScratchBytes = 16u << 20;  // 16 MiB per device
+constexpr size_t kNoallocGroupBytes = 1u << 20;     // group tables up to 1 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+static unsigned char* g_noalloc_scratch_addr[64];   // device address of the array, per device
+
+// Set-up, once per device with that device current: the device address of g_noalloc_scratch (its
+// name in host code is only a host-side stand-in and must never be passed to a kernel).
+static int noalloc_scratch_address(unsigned char** out) {
+  int dev = 0;
+  if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return LS_GPU_ERR_CUDA;
+  if (dev < 0 || dev >= 64) return fail(LS_GPU_ERR_INVALID, "device ordinal out of range");
+  if (g_noalloc_scratch_addr[dev] == nullptr) {
+    void* p = nullptr;
+    if (!cuda_ok(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(g_noalloc_scratch)"))
+      return LS_GPU_ERR_CUDA;
+    g_noalloc_scratch_addr[dev] = (unsigned char*)p;
+  }
+  *out = g_noalloc_scratch_addr[dev];
+  return 0;
+}
+
+template <int DEPTH>
+__device__ inline uint32_t enum_tile_flags(const DeviceGroup& g, const EnumArgs& a, int64_t first, int* cnt) {
+  uint32_t bits = 0;
+  *cnt = 0;
+  if (first < a.n_candidates) {
+    uint64_t v = candidate_at(a, first);
+    const int todo = (int)min((int64_t)kEnumPerThread, a.n_candidates - first);
+    for (int k = 0; k < todo; ++k) {
+      IsRepResult r = is_rep<DEPTH>(g, v, a.lane_width, true);
+      const bool keep = r.ok && (a.reference_rule ? (r.sum > 0) : (r.trivial && r.exact_count > 0));
+      if (keep) {
+        bits |= 1u << k;
+        ++*cnt;
+      }
+      if (k + 1 < todo) v = candidate_next(a, v);
+    }
+  }
+  return bits;
+}
+
+template <int DEPTH>
+__global__ void __launch_bounds__(kEnumThreads) k_enumerate_count(DeviceGroup g, EnumArgs a,
+                                                                  int32_t* __restrict__ tile_count) {
+  __shared__ int64_t warp_sums[32];
+  __shared__ int64_t total;
+  for (int64_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+    int cnt = 0;
+    enum_tile_flags<DEPTH>(g, a, tile * kEnumTile + (int64_t)threadIdx.x * kEnumPerThread, &cnt);
+    block_exclusive_scan((int64_t)cnt, warp_sums, &total);
+    if (threadIdx.x == 0) tile_count[tile] = (int32_t)total;
+    __syncthreads();
+  }
+}
+
+template <int DEPTH>
+__global__ void __launch_bounds__(kEnumThreads) k_enumerate_write(DeviceGroup g, EnumArgs a,
+                                                                  const int64_t* __restrict__ tile_offset,
+                                                                  uint64_t* __restrict__ out, int64_t capacity) {
+  __shared__ int64_t warp_sums[32];
+  __shared__ int64_t total;
+  for (int64_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+    const int64_t first = tile * kEnumTile + (int64_t)threadIdx.x * kEnumPerThread;
+    int cnt = 0;
+    uint32_t bits = enum_tile_flags<DEPTH>(g, a, first, &cnt);
+    const int64_t excl = block_exclusive_scan((int64_t)cnt, warp_sums, &total);
+    if (cnt > 0) {
+      int64_t pos = tile_offset[tile] + excl;
+      uint64_t v = candidate_at(a, first);
+      while (bits != 0) {
+        if (bits & 1u) {
+          if (pos < capacity) out[pos] = v;
+          ++pos;
+        }
+        bits >>= 1;
+        if (bits) v = candidate_next(a, v);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <int D>
+struct RunEnumerateNoalloc {
+  static void run(const DeviceGroup& g, const EnumArgs& a, int32_t* counts, const int64_t* offsets,
+                  uint64_t* out, int64_t capacity, int pass, cudaStream_t s) {
+    int64_t blocks = std::min<int64_t>(a.n_tiles, (int64_t)num_sms() * 8);
+    if (blocks < 1) blocks = 1;
+    if (pass == 0)
+      k_enumerate_count<D><<<(unsigned)blocks, kEnumThreads, 0, s>>>(g, a, counts);
+    else
+      k_enumerate_write<D><<<(unsigned)blocks, kEnumThreads, 0, s>>>(g, a, offsets, out, capacity);
+  }
+};
+
+int enumerate_states_noalloc(const OrbitData* od, const EnumerateRequest& req, uint64_t* d_out,
+                             int64_t capacity, int64_t* count, cudaStream_t s) {
+  *count = 0;
+  if (capacity < 0) return fail(LS_GPU_ERR_INVALID, "negative capacity");
+  if (ensure_binomials() != 0) return LS_GPU_ERR_CUDA;
+  const int n_bits = req.mode == 2 ? 2 * req.number_sites : req.number_sites;
+  if (req.lower > req.upper) return 0;
+  if (req.mode == 1 || req.mode == 2) {
+    // No scratch needed: the states are generated directly from their combinadic ranks.
+    int64_t n = 0, r0 = 0, rA = 0, nA = 0, rB = 0, nB = 0;
+    int h = -1, hA = 0, hB = 0;
+    const int ns = req.number_sites;
+    if (req.mode == 1) {
+      uint64_t low = req.lower, high = req.upper;
+      if (req.spin_inversion != 0) {
+        const uint64_t mask = ns == 0 ? 0 : (~(uint64_t)0) >> (64 - ns);
+        if ((high ^ mask) < high) high ^= mask;
+      }
+      if (low > high) return 0;
+      if (req.hamming_fixed) {
+        h = __builtin_popcountll(low);
+        r0 = fixed_hamming_state_to_index(low);
+        n = fixed_hamming_state_to_index(high) - r0 + 1;
+      } else {
+        r0 = (int64_t)low;
+        n = (int64_t)(high - low) + 1;
+      }
+    } else {
+      const uint64_t mask = ns == 0 ? 0 : (~(uint64_t)0) >> (64 - ns);
+      const uint64_t minA = req.lower & mask, maxA = req.upper & mask;
+      const uint64_t minB = (req.lower >> ns) & mask, maxB = (req.upper >> ns) & mask;
+      hA = __builtin_popcountll(minA);
+      hB = __builtin_popcountll(minB);
+      rA = fixed_hamming_state_to_index(minA);
+      nA = fixed_hamming_state_to_index(maxA) - rA + 1;
+      rB = fixed_hamming_state_to_index(minB);
+      nB = fixed_hamming_state_to_index(maxB) - rB + 1;
+      n = nA * nB;
+    }
+    *count = n;
+    if (n > capacity) return fail(LS_GPU_ERR_INVALID, "output capacity is smaller than the number of states");
+    if (n == 0) return 0;
+    if (req.mode == 1)
+      k_enumerate_plain<<<grid_for((n + 15) / 16, 256), 256, 0, s>>>(r0, n, h, n_bits, d_out);
+    else
+      k_enumerate_spinful<<<grid_for(n / 16 + 1, 256), 256, 0, s>>>(rA, nA, hA, rB, nB, hB, ns, d_out);
+    if (!cuda_ok(cudaGetLastError(), "enumerate (no allocation)")) return LS_GPU_ERR_CUDA;
+    return cuda_ok(cudaStreamSynchronize(s), "enumerate (no allocation)") ? 0 : LS_GPU_ERR_CUDA;
+  }
+  // Projected spin basis: group tables and tile arrays in the static scratch.
+  if (od == nullptr || od->n_elems == 0) return fail(LS_GPU_ERR_INVALID, "projected enumeration without a group");
+  unsigned char* base = nullptr;
+  int rc = noalloc_scratch_address(&base);
+  if (rc != 0) return rc;
+  const size_t group_bytes = od->host_block.size();
+  if (group_bytes > kNoallocGroupBytes)
+    return fail(LS_GPU_ERR_INVALID, "symmetry group tables exceed the 1 MiB reserved for them");
+  EnumArgs a{};
+  a.h = req.hamming_fixed ? __builtin_popcountll(req.lower) : -1;
+  a.n_bits = n_bits;
+  a.lane_width = 4;
+  a.reference_rule = req.reference_norm_rule;
+  if (a.h >= 0) {
+    a.first_rank = fixed_hamming_state_to_index(req.lower);
+    a.n_candidates = fixed_hamming_state_to_index(req.upper) - a.first_rank + 1;
+  } else {
+    a.first_rank = (int64_t)req.lower;
+    a.n_candidates = (int64_t)(req.upper - req.lower) + 1;
+  }
+  a.n_tiles = (a.n_candidates + kEnumTile - 1) / kEnumTile;
+  // tile counts | tile offsets (n + 1) | block sums | scanned block sums (+ total)
+  const int64_t max_tiles =
+      (int64_t)((kNoallocScratchBytes - kNoallocGroupBytes - 4 * 65536) / (4 + 8)) - 1;
+  if (a.n_tiles > max_tiles)
+    return fail(LS_GPU_ERR_INVALID, "basis too large for the allocation-free enumeration (more than " +
+                                        std::to_string(max_tiles * kEnumTile) + " candidate states)");
+  const int64_t n_blocks2 = (a.n_tiles + kScanTile - 1) / kScanTile;
+  if (n_blocks2 > kScanTile) return fail(LS_GPU_ERR_INVALID, "scan too large");
+  unsigned char* p = base + kNoallocGroupBytes;
+  int32_t* counts = (int32_t*)p;
+  p += ((size_t)a.n_tiles * 4 + 255) & ~(size_t)255;
+  int64_t* offsets = (int64_t*)p;
+  p += ((size_t)(a.n_tiles + 1) * 8 + 255) & ~(size_t)255;
+  int64_t* sums = (int64_t*)p;
+  p += ((size_t)(n_blocks2 + 1) * 8 + 255) & ~(size_t)255;
+  int64_t* sums_scan = (int64_t*)p;
+
+  // group view into the scratch (same layout as the orbit data block)
+  if (!cuda_ok(cudaMemcpyAsync(base, od->host_block.data(), group_bytes, cudaMemcpyHostToDevice, s),
+               "copy group tables"))
+    return LS_GPU_ERR_CUDA;
+  DeviceGroup g;
+  g.n_bits = od->n_bits;
+  g.n_elems = od->n_elems;
+  g.depth = od->depth;
+  g.spin_inversion = od->spin_inversion;
+  g.flip = od->n_bits == 0 ? 0 : (~(uint64_t)0) >> (64 - od->n_bits);
+  g.masks_t = (const uint64_t*)(base + od->off_masks);
+  g.shifts = (const uint32_t*)(base + od->off_shifts);
+  g.chars = (const double2*)(base + od->off_chars);
+  g.onehot = (const uint64_t*)(base + od->off_onehot);
+  g.prio = (const uint16_t*)(base + od->off_prio);
+
+  dispatch_depth<RunEnumerateNoalloc>(g.depth, od->standard_shifts, g, a, counts, offsets, d_out, capacity, 0, s);
+  if (!cuda_ok(cudaGetLastError(), "k_enumerate_count")) return LS_GPU_ERR_CUDA;
+  // exclusive scan of the tile counts: per 4096-tile block, then over the block sums
+  k_scan_tiles<int32_t><<<(unsigned)n_blocks2, kScanThreads, 0, s>>>(counts, a.n_tiles, offsets, sums);
+  k_scan_tiles<int64_t><<<1, kScanThreads, 0, s>>>(sums, n_blocks2, sums_scan, sums_scan + n_blocks2);
+  k_scan_add<<<(unsigned)n_blocks2, kScanThreads, 0, s>>>(offsets, a.n_tiles, sums_scan);
+  if (!cuda_ok(cudaMemcpyAsync(offsets + a.n_tiles, sums_scan + n_blocks2, 8, cudaMemcpyDeviceToDevice, s),
+               "scan total"))
+    return LS_GPU_ERR_CUDA;
+  int64_t total = 0;
+  if (!cuda_ok(cudaMemcpyAsync(&total, offsets + a.n_tiles, 8, cudaMemcpyDeviceToHost, s), "read count") ||
+      !cuda_ok(cudaStreamSynchronize(s), "count pass"))
+    return LS_GPU_ERR_CUDA;
+  *count = total;
+  if (total > capacity) return fail(LS_GPU_ERR_INVALID, "output capacity is smaller than the number of states");
+  dispatch_depth<RunEnumerateNoalloc>(g.depth, od->standard_shifts, g, a, counts, offsets, d_out, capacity, 1, s);
+  if (!cuda_ok(cudaGetLastError(), "k_enumerate_write")) return LS_GPU_ERR_CUDA;
+  return cuda_ok(cudaStreamSynchronize(s), "write pass") ? 0 : LS_GPU_ERR_CUDA;
+}
+
 }  // namespace lsg

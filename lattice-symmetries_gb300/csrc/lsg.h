@@ -151,6 +151,10 @@ struct EnumerateRequest {
 // Enumerates into device memory; *d_out is allocated with cudaMalloc (caller frees).
 int enumerate_states(const DeviceGroup* g, const EnumerateRequest& req, uint64_t** d_out,
                      int64_t* count, cudaStream_t s);
+// Enumerates into the caller's d_out (capacity entries) without allocating: all scratch lives in
+// a static device array (see basis.cu).  *count receives the number of states.
+int enumerate_states_noalloc(const OrbitData* od, const EnumerateRequest& req, uint64_t* d_out,
+                             int64_t capacity, int64_t* count, cudaStream_t s);
 
 int build_prefix_index(const uint64_t* d_reps, int64_t n, int number_bits, int prefix_bits,
                        int64_t** d_offsets, int64_t* range_size, int* shift, cudaStream_t s,
