@@ -34,6 +34,13 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 if REPO not in sys.path:
     sys.path.insert(0, REPO)
 
+# DRAM bytes (read + write) of one matvec launch from an ncu capture of the same workload, with the
+# integer (ALU) pipe utilisation of that capture; summaries and commands in profiles/.
+NCU_CAPTURES = {
+    "j1j2_6x6": {"traffic": 117.884e9 + 0.272e9, "alu_pipe_pct": 66.9,
+                 "source": "profiles/k_matvec_packed_j1j2_6x6.md"},
+}
+
 CONFIGS = {
     "j1j2_6x6": dict(L=6, kx=3, ky=3, J2=0.5, inversion=1, seed=2,
                      description="J1-J2 Heisenberg 6x6 torus, J2=0.5, Sz=0, T(36)xC4v(8)xZ2, (pi,pi) sector"),
@@ -244,6 +251,41 @@ def run_reference(args):
     return 0
 
 
+def block_and_adjoint(op, rng, D, elements, ms_per_step, steps, x, y, sptr):
+    """Block H*X with 16 right-hand sides and the adjoint H^dagger x, timed per vector."""
+    import torch
+    stream = torch.cuda.current_stream()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    extra = {}
+    K16 = 16
+    X16 = torch.from_numpy(rng.normal(size=(D, K16)) + 1j * rng.normal(size=(D, K16))).cuda()
+    Y16 = torch.empty_like(X16)
+    for _ in range(2):
+        op.apply_device(X16, out=Y16, stream=sptr, check=False)
+    torch.cuda.synchronize()
+    nb = max(1, steps // 2)
+    start.record(stream)
+    for _ in range(nb):
+        op.apply_device(X16, out=Y16, stream=sptr, check=False)
+    end.record(stream)
+    torch.cuda.synchronize()
+    t16 = start.elapsed_time(end) / nb
+    extra["block16"] = {"ms_per_block": t16, "value_per_vector": elements * K16 / (t16 * 1e-3),
+                        "speedup_per_vector_vs_plain": ms_per_step * K16 / t16}
+    for _ in range(2):
+        op.apply_device(x, out=y, adjoint=True, stream=sptr, check=False)
+    torch.cuda.synchronize()
+    start.record(stream)
+    for _ in range(nb):
+        op.apply_device(x, out=y, adjoint=True, stream=sptr, check=False)
+    end.record(stream)
+    torch.cuda.synchronize()
+    ta = start.elapsed_time(end) / nb
+    extra["adjoint"] = {"ms_per_step": ta, "value": elements / (ta * 1e-3)}
+    op.check_errors(sptr)
+    return extra
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -254,6 +296,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the block-16 and adjoint lines")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -278,7 +322,7 @@ def main():
     D = basis.number_states
     nnz = op.count_nonzeros()
     elements = D + nnz
-    tuned = op.autotune(1)
+    tuned = (None, None, None) if args.no_autotune else op.autotune(1)
     rng = np.random.default_rng(CONFIGS[args.config]["seed"])
     x_host = rng.normal(size=D) + 1j * rng.normal(size=D)
     x = torch.from_numpy(x_host).cuda()
@@ -317,33 +361,7 @@ def main():
     peak, peak_kind = load_peaks()
 
     # block matvec (16 right-hand sides) and adjoint, per vector
-    extra = {}
-    K16 = 16
-    X16 = torch.from_numpy(rng.normal(size=(D, K16)) + 1j * rng.normal(size=(D, K16))).cuda()
-    Y16 = torch.empty_like(X16)
-    for _ in range(2):
-        op.apply_device(X16, out=Y16, stream=sptr, check=False)
-    torch.cuda.synchronize()
-    nb = max(1, args.steps // 2)
-    start.record(stream)
-    for _ in range(nb):
-        op.apply_device(X16, out=Y16, stream=sptr, check=False)
-    end.record(stream)
-    torch.cuda.synchronize()
-    t16 = start.elapsed_time(end) / nb
-    extra["block16"] = {"ms_per_block": t16, "value_per_vector": elements * K16 / (t16 * 1e-3),
-                        "speedup_per_vector_vs_plain": ms_per_step * K16 / t16}
-    for _ in range(2):
-        op.apply_device(x, out=y, adjoint=True, stream=sptr, check=False)
-    torch.cuda.synchronize()
-    start.record(stream)
-    for _ in range(nb):
-        op.apply_device(x, out=y, adjoint=True, stream=sptr, check=False)
-    end.record(stream)
-    torch.cuda.synchronize()
-    ta = start.elapsed_time(end) / nb
-    extra["adjoint"] = {"ms_per_step": ta, "value": elements / (ta * 1e-3)}
-    op.check_errors(sptr)
+    extra = {} if args.no_extras else block_and_adjoint(op, rng, D, elements, ms_per_step, args.steps, x, y, sptr)
 
     # end to end through the reference-facing C ABI with host buffers
     e2e = None
@@ -378,8 +396,12 @@ def main():
                        "number_states": D, "nnz": nnz, "rhs": 1, "parallelism": "replicas",
                        "l2": "inputs larger than L2 (x 16 B/state, representatives + norms + index)"},
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",
-                         "frac": achieved_gbs / peak, "traffic": None, "peak_source": peak_kind,
-                         "note": "integer-pipe bound orbit scan; HBM fraction of algorithmic bytes"},
+                         "frac": achieved_gbs / peak, "peak_source": peak_kind,
+                         "traffic": NCU_CAPTURES.get(args.config, {}).get("traffic"),
+                         "alu_pipe_pct": NCU_CAPTURES.get(args.config, {}).get("alu_pipe_pct"),
+                         "bytes_per_launch": bytes_per_launch,
+                         "note": "integer-ALU bound orbit scan (alu_pipe_pct from ncu); frac is of algorithmic "
+                                 "bytes, traffic is ncu DRAM bytes per launch"},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
             "clocks": clocks.summary(), "basis_build_s": t_build, "extra": extra,
             "autotune": {"threads": tuned[0], "waves": tuned[1], "ms": tuned[2]},
