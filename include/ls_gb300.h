@@ -298,10 +298,37 @@ int ls_gpu_coupling_inner_products(ls_hs_operator const *op, int n_couplings,
                                    int32_t const *term_coupling, double const *d_g,
                                    double const *d_x, double *d_out, void *stream);
 
-/* Multi-sector block matvec: one persistent launch over `n_sectors` operators (same term
- * structure, different bases/characters), each with its own x/y block of k right-hand sides.
- * Work tiles (sector, rows) are claimed from a device counter.  d_x[s], d_y[s] are device
- * pointers with leading dimension k. */
+/* Membership rule of the projected enumeration behind ls_hs_build_representatives and
+ * ls_chpl_enumerate_representatives: 0 (default) keeps a state iff the reference's floating
+ * stabiliser sum is positive (StatesEnumeration.chpl:242-268), 1 iff its stabiliser has only
+ * trivial characters (exact).  They differ only in complex sectors, where the floating rule keeps
+ * rounding residue: representatives whose exact norm is zero.  The matvec treats such states as
+ * zero rows and columns.  Returns the previous rule.  No counterpart in the reference. */
+int ls_gpu_set_enumeration_rule(int exact);
+
+/* Batched multi-sector block matvec y_s = H_s x_s (or H_s^dagger x_s), complex128, for many
+ * symmetry sectors at once.  No reference counterpart: the reference applies one operator to one
+ * real vector per call (DistributedMatrixVector.chpl:1096-1097).
+ *
+ * A plan fixes the operators (one per sector, each on its own built basis), k right-hand sides and
+ * the device vectors: d_x[s], d_y[s] point to [D_s][ld] complex128 blocks.  When all sectors share
+ * the group's site images, the terms and the particle-number constraint (the usual case: the same
+ * Hamiltonian in different momentum / inversion sectors of one group), each chunk of up to 16
+ * right-hand sides is ONE persistent kernel launch over the rows of all sectors, so uneven sector
+ * sizes balance across the GPU; otherwise the plan launches the sectors one after the other
+ * (ls_gpu_sector_plan_is_batched tells which).  Running a plan allocates nothing and does not
+ * synchronise: it may be captured in a CUDA graph (make one uncaptured run first).  A plan keeps
+ * device pointers of the operators' uploaded tables: changing an operator's terms invalidates it
+ * (run then fails).  Errors of generated states (wrong particle number) go to the device error
+ * word: check with ls_gpu_check_errors. */
+int ls_gpu_sector_plan_create(int n_sectors, ls_hs_operator const *const *ops, int k,
+                              double const *const *d_x, int64_t ldx, double *const *d_y,
+                              int64_t ldy, int adjoint, void **plan);
+int ls_gpu_sector_plan_run(void const *plan, void *stream);
+int ls_gpu_sector_plan_is_batched(void const *plan);
+int ls_gpu_sector_plan_destroy(void *plan);
+
+/* One-shot form of the above (leading dimension k); synchronises `stream` before returning. */
 int ls_gpu_matvec_multi_sector_c128(int n_sectors, ls_hs_operator const *const *ops, int k,
                                     double const *const *d_x, double *const *d_y, int adjoint,
                                     void *stream);

@@ -5,6 +5,9 @@ Python identifier).  The public names mirror the reference's ``lattice_symmetrie
 
     Symmetry, Symmetries, SpinBasis, SpinfulFermionBasis, SpinlessFermionBasis, Expr, Operator
 
+plus the batched GPU additions SectorBatch (many symmetry sectors in one launch) and the
+block-Lanczos driver in ``lanczos``.
+
 All numeric work (orbit scan, basis enumeration, state index, H*x) runs in libls_gb300.so on the
 GPU; importing this package fails if that library has not been built.
 """
@@ -12,7 +15,7 @@ GPU; importing this package fails if that library has not been built.
 from ._group import Symmetry, Symmetries  # noqa: F401
 from ._expr import Expr  # noqa: F401
 from . import _native  # noqa: F401
-from ._api import (Basis, Operator, SpinBasis, SpinfulFermionBasis,  # noqa: F401
+from ._api import (Basis, Operator, SectorBatch, SpinBasis, SpinfulFermionBasis,  # noqa: F401
                    SpinlessFermionBasis, load_library)
 
 __version__ = "2.2.0+gb300"

@@ -147,13 +147,21 @@ class Basis:
     def _estimates(self) -> Tuple[int, int]:
         raise NotImplementedError
 
-    def build(self) -> None:
-        """Generate the sorted list of representatives on the GPU (ls_hs_basis_build)."""
+    def build(self, exact_norms: bool = False) -> None:
+        """Generate the sorted list of representatives on the GPU (ls_hs_basis_build).
+
+        exact_norms=False keeps the reference's membership rule (floating stabiliser sum > 0);
+        exact_norms=True drops the states whose exact orbit norm is zero, which the floating rule
+        can keep in complex sectors as rounding residue."""
         if not self.is_built:
             if self.number_bits > 64:
                 raise RuntimeError("too many bits")
             lo, hi = self._estimates()
-            self._lib.ls_hs_build_representatives(self._payload, lo, hi)
+            previous = self._lib.ls_gpu_set_enumeration_rule(int(bool(exact_norms)))
+            try:
+                self._lib.ls_hs_build_representatives(self._payload, lo, hi)
+            finally:
+                self._lib.ls_gpu_set_enumeration_rule(previous)
             N.check()
         assert self.is_built
 
@@ -613,3 +621,103 @@ class Operator(_LinearOperator):
 
 def load_library():
     return N.lib()
+
+
+class SectorBatch:
+    """H_s X_s for many symmetry sectors s at once (the batched form of Operator.apply_device).
+
+    ``operators`` holds one Operator per sector, each on its own built basis (typically the same
+    Hamiltonian in all momentum / spin-inversion sectors of one group).  The batch owns two
+    zero-padded complex128 tensors ``X`` and ``Y`` of shape [n_sectors, D_max, k]; sector s uses
+    the rows [0, D_s) of ``X[s]`` and ``Y[s]`` (``x(s)``, ``y(s)`` are those views) and padding rows
+    stay zero.  ``run()`` computes Y = H X (or H^dagger X) with one persistent kernel launch per
+    chunk of up to 16 right-hand sides over the rows of all sectors (``batched`` says whether the
+    sectors could share one launch); ``capture()`` records that launch in a CUDA graph and
+    ``replay()`` re-launches it.  No reference counterpart: the reference applies one operator to
+    one real vector per call (DistributedMatrixVector.chpl:1096-1097).
+    """
+
+    def __init__(self, operators: List["Operator"], k: int = 1, adjoint: bool = False, device=None):
+        import torch
+
+        if len(operators) == 0:
+            raise ValueError("need at least one operator")
+        for op in operators:
+            op._check_basis_is_built("SectorBatch")
+        self._ops = list(operators)
+        self._lib = N.lib()
+        self.k = int(k)
+        self.adjoint = bool(adjoint)
+        self.sizes = [op.basis.number_states for op in operators]
+        self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        d_max = max(max(self.sizes), 1)
+        self.X = torch.zeros((len(operators), d_max, self.k), dtype=torch.complex128, device=self.device)
+        self.Y = torch.zeros_like(self.X)
+        n = len(operators)
+        ops_arr = (POINTER(N.ls_hs_operator) * n)(*[op._payload for op in operators])
+        xs = (c_void_p * n)(*[self.X[s].data_ptr() for s in range(n)])
+        ys = (c_void_p * n)(*[self.Y[s].data_ptr() for s in range(n)])
+        plan = c_void_p(0)
+        with torch.cuda.device(self.device):
+            rc = self._lib.ls_gpu_sector_plan_create(n, ops_arr, self.k, xs, self.k, ys, self.k,
+                                                     int(self.adjoint), byref(plan))
+        N.check(rc, "sector plan")
+        self._plan = plan
+        self.batched = bool(self._lib.ls_gpu_sector_plan_is_batched(plan))
+        self._graph = None
+
+    def __del__(self):
+        try:
+            if getattr(self, "_plan", None) is not None and self._plan.value:
+                self._lib.ls_gpu_sector_plan_destroy(self._plan)
+                self._plan = None
+        except Exception:
+            pass
+
+    @property
+    def number_sectors(self) -> int:
+        return len(self._ops)
+
+    def x(self, s: int):
+        return self.X[s, : self.sizes[s]]
+
+    def y(self, s: int):
+        return self.Y[s, : self.sizes[s]]
+
+    def run(self, stream=None, check: bool = False):
+        """Enqueues Y = H X on `stream` (default: torch's current stream); check=True synchronises
+        and raises on a generated state outside its basis."""
+        import torch
+
+        if stream is None:
+            stream = torch.cuda.current_stream(self.device).cuda_stream
+        N.check(self._lib.ls_gpu_sector_plan_run(self._plan, stream), "sector matvec")
+        if check:
+            N.check(self._lib.ls_gpu_check_errors(stream), "sector matvec")
+        return self.Y
+
+    def capture(self):
+        """Records run() in a CUDA graph (after one uncaptured run that uploads every table)."""
+        import torch
+
+        self.run(check=True)
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self.run(stream=s.cuda_stream)
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        self._graph = g
+        return g
+
+    def replay(self):
+        if self._graph is None:
+            self.capture()
+        self._graph.replay()
+        return self.Y
+
+    def check_errors(self):
+        import torch
+        N.check(self._lib.ls_gpu_check_errors(torch.cuda.current_stream(self.device).cuda_stream), "sector matvec")

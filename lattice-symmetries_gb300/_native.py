@@ -160,6 +160,12 @@ _SIGNATURES = [
                                                c_void_p, c_void_p, c_void_p]),
     ("ls_gpu_matvec_multi_sector_c128", c_int, [c_int, POINTER(POINTER(ls_hs_operator)), c_int,
                                                 POINTER(c_void_p), POINTER(c_void_p), c_int, c_void_p]),
+    ("ls_gpu_sector_plan_create", c_int, [c_int, POINTER(POINTER(ls_hs_operator)), c_int, POINTER(c_void_p),
+                                          c_int64, POINTER(c_void_p), c_int64, c_int, POINTER(c_void_p)]),
+    ("ls_gpu_sector_plan_run", c_int, [c_void_p, c_void_p]),
+    ("ls_gpu_set_enumeration_rule", c_int, [c_int]),
+    ("ls_gpu_sector_plan_is_batched", c_int, [c_void_p]),
+    ("ls_gpu_sector_plan_destroy", c_int, [c_void_p]),
     ("ls_gpu_state_info", c_int, [POINTER(ls_hs_basis), c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("ls_gpu_is_representative", c_int, [POINTER(ls_hs_basis), c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("ls_gpu_state_index", c_int, [POINTER(ls_hs_basis), c_int64, c_void_p, c_void_p, c_void_p]),

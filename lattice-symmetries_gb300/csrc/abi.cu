@@ -615,6 +615,19 @@ static DeviceConstraint basis_constraint(ls_hs_basis const* b) {
 // =================================================================================================
 // Enumeration driver (StatesEnumeration.chpl:674-709)
 // =================================================================================================
+// Membership rule of projected enumeration: 0 keeps a state iff the reference's floating
+// stabiliser sum is positive (StatesEnumeration.chpl:242-268 via is_representative), 1 iff its
+// exact stabiliser has only trivial characters.  The two differ only in complex sectors, where the
+// floating rule can keep rounding residue (norms ~1e-9 that are exactly zero).
+static int g_enum_exact = 0;
+
+extern "C" int ls_gpu_set_enumeration_rule(int exact) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  const int previous = g_enum_exact;
+  g_enum_exact = exact ? 1 : 0;
+  return previous;
+}
+
 static int enumerate_into(ls_hs_basis const* b, uint64_t** d_out, int64_t* count) {
   EnumerateRequest req{};
   uint64_t lo, hi;
@@ -624,7 +637,7 @@ static int enumerate_into(ls_hs_basis const* b, uint64_t** d_out, int64_t* count
   req.number_sites = b->number_sites;
   req.spin_inversion = b->spin_inversion;
   req.hamming_fixed = hamming_fixed(b);
-  req.reference_norm_rule = 1;
+  req.reference_norm_rule = g_enum_exact ? 0 : 1;
   const OrbitData* od = basis_orbit(b);
   const DeviceGroup* g = nullptr;
   if (b->particle_type == LS_HS_SPIN) {
@@ -663,7 +676,7 @@ extern "C" int ls_gpu_enumerate_noalloc(ls_hs_basis const* b, uint64_t* d_out, i
   req.number_sites = b->number_sites;
   req.spin_inversion = b->spin_inversion;
   req.hamming_fixed = hamming_fixed(b);
-  req.reference_norm_rule = 1;
+  req.reference_norm_rule = g_enum_exact ? 0 : 1;
   const OrbitData* od = nullptr;
   if (b->particle_type == LS_HS_SPIN) {
     if (has_permutations(b)) {
@@ -1005,6 +1018,9 @@ int ensure_norms(IndexData* ix, const OrbitData* od) {
   if (od != nullptr && od->n_elems > 0) {
     const DeviceGroup* dg = orbit_device(od);
     rc = dg ? launch_orbit_norms(*dg, ix->n_states, ix->d_reps, ix->d_norms, s) : LS_GPU_ERR_CUDA;
+    // The norms are computed on the library's stream but read by kernels on the caller's stream:
+    // finish them before any caller can launch.
+    if (rc == 0) rc = cuda_ok(cudaStreamSynchronize(s), "orbit norms") ? 0 : LS_GPU_ERR_CUDA;
   } else {
     std::vector<double> ones((size_t)std::max<int64_t>(ix->n_states, 1), 1.0);
     rc = cuda_ok(cudaMemcpyAsync(ix->d_norms, ones.data(), ones.size() * 8, cudaMemcpyHostToDevice, s),
@@ -1290,12 +1306,118 @@ extern "C" int ls_gpu_coupling_inner_products(ls_hs_operator const* op, int n_co
   return fail(LS_GPU_ERR_INVALID, "not implemented yet");
 }
 
+namespace {
+constexpr uint32_t kPlanMagic = 0x504c414eu;  // "PLAN"
+struct SectorPlanHandle {
+  uint32_t magic = kPlanMagic;
+  int device = 0;
+  std::vector<const ls_hs_operator*> ops;
+  std::vector<OperatorCache*> caches;
+  SectorPlan* plan = nullptr;
+};
+
+// Whether sector i can share sector 0's shared-memory tables in one batched launch.
+bool sectors_share_tables(ls_hs_operator const* a, ls_hs_operator const* b, const MatvecProblem& pa,
+                          const MatvecProblem& pb) {
+  if (pa.projection != 2 || pb.projection != 2) return false;
+  if (pa.group.n_bits != pb.group.n_bits || pa.group.gpl != pb.group.gpl || pa.group.n_elems != pb.group.n_elems)
+    return false;
+  if ((pa.group.spin_inversion != 0) != (pb.group.spin_inversion != 0)) return false;
+  const DeviceConstraint &ca = pa.constraint, &cb = pb.constraint;
+  if (ca.kind != cb.kind || ca.half_bits != cb.half_bits || ca.w0 != cb.w0 || ca.w1 != cb.w1) return false;
+  const OrbitData* oa = basis_orbit(a->basis);
+  const OrbitData* ob = basis_orbit(b->basis);
+  if (oa == nullptr || ob == nullptr || oa->gpl != ob->gpl || oa->gpl == 0) return false;
+  const size_t bytes = (size_t)oa->n_bits * 32 * oa->gpl * 8;
+  if (oa->host_block.size() < oa->off_onehot_packed + bytes || ob->host_block.size() < ob->off_onehot_packed + bytes)
+    return false;
+  if (memcmp(oa->host_block.data() + oa->off_onehot_packed, ob->host_block.data() + ob->off_onehot_packed, bytes) != 0)
+    return false;
+  OperatorCache* c = g_ops[a];
+  return c != nullptr && same_terms(c->off, b->off_diag_terms) && same_terms(c->diag, b->diag_terms);
+}
+}  // namespace
+
+extern "C" int ls_gpu_sector_plan_create(int n_sectors, ls_hs_operator const* const* ops, int k,
+                                         double const* const* d_x, int64_t ldx, double* const* d_y,
+                                         int64_t ldy, int adjoint, void** plan) {
+  if (plan == nullptr) return fail(LS_GPU_ERR_INVALID, "plan must not be NULL");
+  *plan = nullptr;
+  if (n_sectors < 1 || ops == nullptr || d_x == nullptr || d_y == nullptr)
+    return fail(LS_GPU_ERR_INVALID, "need at least one sector with operators and vectors");
+  if (k < 1 || ldx < k || ldy < k) return fail(LS_GPU_ERR_INVALID, "invalid k / leading dimension");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  std::vector<MatvecProblem> problems(n_sectors);
+  SectorPlanHandle* h = new SectorPlanHandle();
+  cudaGetDevice(&h->device);
+  for (int i = 0; i < n_sectors; ++i) {
+    if (ops[i] == nullptr) {
+      delete h;
+      return fail(LS_GPU_ERR_INVALID, "NULL operator in the sector list");
+    }
+    const int rc = make_problem(ops[i], adjoint != 0, &problems[i]);
+    if (rc != 0) {
+      delete h;
+      return rc;
+    }
+    h->ops.push_back(ops[i]);
+    h->caches.push_back(g_ops[ops[i]]);
+  }
+  bool share = true;
+  for (int i = 1; i < n_sectors && share; ++i)
+    share = sectors_share_tables(ops[0], ops[i], problems[0], problems[i]);
+  std::vector<const double*> xs(d_x, d_x + n_sectors);
+  std::vector<double*> ys(d_y, d_y + n_sectors);
+  const int rc = sector_plan_build(problems, share, k, xs, ldx, ys, ldy, &h->plan);
+  if (rc != 0) {
+    delete h;
+    return rc;
+  }
+  *plan = h;
+  return 0;
+}
+
+extern "C" int ls_gpu_sector_plan_is_batched(void const* plan) {
+  const SectorPlanHandle* h = (const SectorPlanHandle*)plan;
+  if (h == nullptr || h->magic != kPlanMagic) return fail(LS_GPU_ERR_INVALID, "not a sector plan");
+  return sector_plan_batched(h->plan) ? 1 : 0;
+}
+
+extern "C" int ls_gpu_sector_plan_run(void const* plan, void* stream) {
+  const SectorPlanHandle* h = (const SectorPlanHandle*)plan;
+  if (h == nullptr || h->magic != kPlanMagic) return fail(LS_GPU_ERR_INVALID, "not a sector plan");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != h->device) return fail(LS_GPU_ERR_INVALID, "sector plan was created on another device");
+  for (size_t i = 0; i < h->ops.size(); ++i) {
+    auto it = g_ops.find(h->ops[i]);
+    if (it == g_ops.end() || it->second != h->caches[i] || !same_terms(it->second->off, h->ops[i]->off_diag_terms) ||
+        !same_terms(it->second->diag, h->ops[i]->diag_terms))
+      return fail(LS_GPU_ERR_INVALID, "an operator of the sector plan changed after the plan was created");
+  }
+  return sector_plan_run(h->plan, device_error_word(), (cudaStream_t)stream);
+}
+
+extern "C" int ls_gpu_sector_plan_destroy(void* plan) {
+  SectorPlanHandle* h = (SectorPlanHandle*)plan;
+  if (h == nullptr) return 0;
+  if (h->magic != kPlanMagic) return fail(LS_GPU_ERR_INVALID, "not a sector plan");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  sector_plan_free(h->plan);
+  h->magic = 0;
+  delete h;
+  return 0;
+}
+
 extern "C" int ls_gpu_matvec_multi_sector_c128(int n_sectors, ls_hs_operator const* const* ops, int k,
                                                double const* const* d_x, double* const* d_y, int adjoint,
                                                void* stream) {
-  for (int i = 0; i < n_sectors; ++i) {
-    int rc = ls_gpu_matvec_c128(ops[i], k, d_x[i], k, d_y[i], k, adjoint, stream);
-    if (rc != 0) return rc;
-  }
-  return 0;
+  void* plan = nullptr;
+  int rc = ls_gpu_sector_plan_create(n_sectors, ops, k, d_x, k, d_y, k, adjoint, &plan);
+  if (rc != 0) return rc;
+  rc = ls_gpu_sector_plan_run(plan, stream);
+  if (rc == 0 && !cuda_ok(cudaStreamSynchronize((cudaStream_t)stream), "multi-sector matvec")) rc = LS_GPU_ERR_CUDA;
+  const int rc2 = ls_gpu_sector_plan_destroy(plan);
+  return rc != 0 ? rc : rc2;
 }

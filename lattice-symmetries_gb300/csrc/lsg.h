@@ -183,14 +183,18 @@ struct MatvecProblem {
 int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, int64_t ldx,
                   double* d_y, int64_t ldy, int* d_err, cudaStream_t s);
 
-struct MultiSectorProblem {
-  int n_sectors;
-  const MatvecProblem* problems;   // host array
-  int k;
-  const double* const* d_x;        // host array of device pointers
-  double* const* d_y;
-};
-int launch_matvec_multi(const MultiSectorProblem& mp, int* d_err, cudaStream_t s);
+// Sector plans (matvec.cu): y_s = H_s x_s (complex, k right-hand sides, leading dimensions
+// ldx/ldy) for many sectors.  When the sectors share the group's site images, the terms and the
+// constraint (`shareable`), each RHS chunk is ONE persistent launch over all sectors' rows;
+// otherwise the plan launches the sectors one after the other.  Running a plan allocates nothing
+// and does not synchronise, so it can be captured in a CUDA graph.
+struct SectorPlan;
+int sector_plan_build(const std::vector<MatvecProblem>& problems, bool shareable, int k,
+                      const std::vector<const double*>& xs, int64_t ldx, const std::vector<double*>& ys,
+                      int64_t ldy, SectorPlan** out);
+int sector_plan_run(const SectorPlan* plan, int* d_err, cudaStream_t s);
+bool sector_plan_batched(const SectorPlan* plan);
+void sector_plan_free(SectorPlan* plan);
 
 int launch_coupling_products(const MatvecProblem& p, int n_couplings, const double* d_g,
                              const double* d_x, double* d_out, int* d_err, cudaStream_t s);

@@ -35,6 +35,17 @@ extern const uint64_t* device_binomials();
 
 constexpr size_t kMaxDynamicSmem = 200 * 1024;
 
+LaunchShape packed_shape(int64_t n_rows) {
+  // two resident CTAs per SM; `waves` grids of that size balance the uneven per-row work
+  const int threads = g_threads_override > 0 ? g_threads_override : 320;
+  const int waves = g_blocks_per_sm_override > 0 ? g_blocks_per_sm_override : 8;
+  const int warps_per_block = threads / 32;
+  int64_t blocks = (int64_t)num_sms() * 2 * waves;
+  blocks = std::min<int64_t>(blocks, (n_rows + warps_per_block - 1) / warps_per_block);
+  blocks = std::max<int64_t>(blocks, 1);
+  return LaunchShape{(int)blocks, threads};
+}
+
 // Splits k right-hand sides into launches of 16, 8, 4 and 1 columns.
 int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, int64_t ldx,
                   double* d_y, int64_t ldy, int* d_err, cudaStream_t s) {
@@ -45,14 +56,7 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
   const size_t scalar_words = cplx ? 2 : 1;  // doubles per element
   if (p.projection == 2) {
     const bool inv = p.group.spin_inversion != 0;
-    const int threads = g_threads_override > 0 ? g_threads_override : 256;
-    const int warps_per_block = threads / 32;
-    // two resident CTAs per SM; `waves` grids of that size balance the per-row work
-    const int waves = g_blocks_per_sm_override > 0 ? g_blocks_per_sm_override : 4;
-    int64_t blocks = (int64_t)num_sms() * 2 * waves;
-    blocks = std::min<int64_t>(blocks, (p.n_rows + warps_per_block - 1) / warps_per_block);
-    blocks = std::max<int64_t>(blocks, 1);
-    const LaunchShape sh{(int)blocks, threads};
+    const LaunchShape sh = packed_shape(p.n_rows);
     const PackedLayout PL = make_packed_layout(p);
     const bool packed = p.group.gpl > 0 && p.group.onehot_packed != nullptr && PL.total <= kMaxDynamicSmem;
     if (packed) {
@@ -90,6 +94,112 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
   blocks = std::max<int64_t>(blocks, 1);
   const LaunchShape sh{(int)blocks, threads};
   return launch_plain(cplx, p.projection == 1, k, p, L, sh, d_x, ldx, d_y, ldy, d_err, binom, s);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Sector plans: y_s = H_s x_s for many sectors s in one persistent launch per RHS chunk.
+// ------------------------------------------------------------------------------------------------
+struct SectorPlan {
+  int n_sectors = 0, k = 0;
+  int64_t ldx = 0, ldy = 0;
+  bool batched = false;
+  MatvecProblem shared{};          // tables of the first sector (batched form)
+  PackedLayout layout{};
+  int64_t total_rows = 0;
+  struct Chunk {
+    int k;
+    int col;
+    SectorDesc* d_desc;
+  };
+  std::vector<Chunk> chunks;
+  std::vector<MatvecProblem> problems;  // per-sector form
+  std::vector<const double*> xs;
+  std::vector<double*> ys;
+};
+
+int sector_plan_build(const std::vector<MatvecProblem>& problems, bool shareable, int k,
+                      const std::vector<const double*>& xs, int64_t ldx, const std::vector<double*>& ys,
+                      int64_t ldy, SectorPlan** out) {
+  *out = nullptr;
+  const int n = (int)problems.size();
+  SectorPlan* plan = new SectorPlan();
+  plan->n_sectors = n;
+  plan->k = k;
+  plan->ldx = ldx;
+  plan->ldy = ldy;
+  plan->problems = problems;
+  plan->xs = xs;
+  plan->ys = ys;
+  const MatvecProblem& p0 = problems[0];
+  plan->batched = shareable && n <= kMaxSectors && p0.projection == 2 && p0.group.gpl >= 1 &&
+                  p0.group.gpl <= kSectorMaxGpl && p0.group.onehot_packed != nullptr;
+  if (plan->batched) {
+    plan->shared = p0;
+    plan->layout = make_packed_layout(p0, n);
+    if (plan->layout.total > kMaxDynamicSmem) plan->batched = false;
+  }
+  if (plan->batched) {
+    std::vector<SectorDesc> h(n);
+    int64_t rows = 0;
+    for (int i = 0; i < n; ++i) {
+      h[i].index = problems[i].index;
+      h[i].chars = problems[i].group.chars_packed;
+      h[i].row_begin = rows;
+      h[i].spin_inversion = problems[i].group.spin_inversion;
+      rows += problems[i].n_rows;
+    }
+    plan->total_rows = rows;
+    int done = 0;
+    while (done < k) {
+      const int left = k - done;
+      const int chunk = left >= 16 ? 16 : left >= 8 ? 8 : left >= 4 ? 4 : 1;
+      for (int i = 0; i < n; ++i) {
+        h[i].x = xs[i] + (size_t)done * 2;
+        h[i].y = ys[i] + (size_t)done * 2;
+      }
+      SectorDesc* d = nullptr;
+      if (!cuda_ok(cudaMalloc((void**)&d, (size_t)n * sizeof(SectorDesc)), "cudaMalloc(sector table)") ||
+          !cuda_ok(cudaMemcpy(d, h.data(), (size_t)n * sizeof(SectorDesc), cudaMemcpyHostToDevice),
+                   "upload sector table")) {
+        sector_plan_free(plan);
+        return LS_GPU_ERR_CUDA;
+      }
+      plan->chunks.push_back({chunk, done, d});
+      done += chunk;
+    }
+  }
+  *out = plan;
+  return 0;
+}
+
+bool sector_plan_batched(const SectorPlan* plan) { return plan != nullptr && plan->batched; }
+
+int sector_plan_run(const SectorPlan* plan, int* d_err, cudaStream_t s) {
+  if (!plan->batched) {
+    for (int i = 0; i < plan->n_sectors; ++i) {
+      const int rc = launch_matvec(plan->problems[i], Scalar::Complex, plan->k, plan->xs[i], plan->ldx,
+                                   plan->ys[i], plan->ldy, d_err, s);
+      if (rc != 0) return rc;
+    }
+    return 0;
+  }
+  const uint64_t* binom = device_binomials();
+  if (binom == nullptr) return LS_GPU_ERR_CUDA;
+  if (plan->total_rows == 0) return 0;
+  const LaunchShape sh = packed_shape(plan->total_rows);
+  const bool inv = plan->shared.group.spin_inversion != 0;
+  for (const SectorPlan::Chunk& c : plan->chunks) {
+    const int rc = launch_sectors(c.k, plan->shared.group.gpl, inv, plan->shared, plan->layout, sh, c.d_desc,
+                                  plan->n_sectors, plan->total_rows, plan->ldx, plan->ldy, d_err, binom, s);
+    if (rc != 0) return rc;
+  }
+  return 0;
+}
+
+void sector_plan_free(SectorPlan* plan) {
+  if (plan == nullptr) return;
+  for (const SectorPlan::Chunk& c : plan->chunks) cudaFree(c.d_desc);
+  delete plan;
 }
 
 }  // namespace lsg

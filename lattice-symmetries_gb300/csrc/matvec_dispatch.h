@@ -33,6 +33,17 @@ LSG_DECLARE_PACKED(launch_packed_cplx_k4)
 LSG_DECLARE_PACKED(launch_packed_cplx_k8)
 LSG_DECLARE_PACKED(launch_packed_cplx_k16)
 
+// Batched multi-sector kernel (complex, k in {1, 4, 8, 16}, gpl in {1, 2, 3, 4}).
+struct SectorDesc;
+int launch_sectors(int k, int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L, LaunchShape sh,
+                   const SectorDesc* d_desc, int n_sectors, int64_t total_rows, int64_t ldx, int64_t ldy,
+                   int* err, const uint64_t* binom, cudaStream_t s);
+constexpr int kSectorMaxGpl = 4;
+constexpr int kMaxSectors = 256;
+
+// Launch shape of the warp-per-row kernels: threads per block and grid waves (settable).
+LaunchShape packed_shape(int64_t n_rows);
+
 // Unprojected / spin-inversion-only kernel.
 int launch_plain(bool cplx, bool inv, int k, const MatvecProblem& p, const SmemLayout& L,
                  LaunchShape sh, const double* x, int64_t ldx, double* y, int64_t ldy, int* err,

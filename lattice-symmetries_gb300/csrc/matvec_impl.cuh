@@ -206,6 +206,13 @@ __global__ void __launch_bounds__(256, 2)
   for (int64_t row = warp_id; row < p.n_rows; row += n_warps) {
     const uint64_t a = __ldg(p.index.reps + row);
     const double na = __ldg(p.index.norms + row);
+    if (na == 0.0) {  // zero-norm representative: zero row and column (see packed_row)
+      if (lane < K) {
+        if constexpr (CPLX) reinterpret_cast<double2*>(y)[row * ldy + lane] = make_double2(0.0, 0.0);
+        else y[row * ldy + lane] = 0.0;
+      }
+      continue;
+    }
 
     // g.a for my elements
     uint64_t ga[GPL];
@@ -243,11 +250,13 @@ __global__ void __launch_bounds__(256, 2)
       double fre = 0.0, fim = 0.0;
       if (lane < nslot) {
         j = mv_index_lookup(p.index, my_rep, binom);
+        const double nj = j >= 0 ? __ldg(p.index.norms + j) : 0.0;
+        if (nj == 0.0) j = -1;  // zero-norm column
         found += (j >= 0);
         if (j >= 0) {
           double2 chi = S.chars[my_idx >> 1];
           if (INV && (my_idx & 1) && p.group.spin_inversion == -1) chi = make_double2(-chi.x, -chi.y);
-          const double ratio = __ldg(p.index.norms + j) / na;
+          const double ratio = nj / na;
           const C2 f = cmul_conj_b(C2{my_c.x, my_c.y}, C2{chi.x, chi.y});
           fre = f.re * ratio;
           fim = f.im * ratio;
@@ -366,16 +375,30 @@ __global__ void __launch_bounds__(256, 2)
 // ------------------------------------------------------------------------------------------------
 struct PackedLayout {
   size_t off_onehot, off_chars, off_tm, off_tl, off_tx, off_ts, off_tv, off_ti, off_dm, off_dr, off_ds, off_dv;
+  size_t off_sectors;  // sector table of the batched kernel (n_sectors > 0)
   size_t total;
 };
 
-inline PackedLayout make_packed_layout(const MatvecProblem& p) {
+// One symmetry sector of a batched launch: its states, index, norms, characters and vectors.
+// All sectors of a batch share the group's site images, the operator's terms and the basis
+// constraint; they differ in the representatives (sector) and the characters.
+struct SectorDesc {
+  DeviceIndex index;
+  const double2* chars;  // packed characters [gpl * 32] (device)
+  const double* x;       // first column of this launch's right-hand sides
+  double* y;
+  int64_t row_begin;     // first row of the sector in the batch's concatenated row space
+  int64_t spin_inversion;
+};
+static_assert(sizeof(SectorDesc) % 8 == 0, "sector descriptors are staged as 64-bit words");
+
+inline PackedLayout make_packed_layout(const MatvecProblem& p, int n_sectors = 0) {
   PackedLayout L{};
   auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
   const size_t Gp = 32 * (size_t)p.group.gpl;
   size_t o = 0;
   L.off_onehot = o; o = al(o + (size_t)p.group.n_bits * Gp * 8);
-  L.off_chars = o; o = al(o + Gp * 16);
+  L.off_chars = o; o = al(o + (n_sectors > 0 ? 0 : Gp * 16));
   L.off_tm = o; o = al(o + (size_t)p.off.n * 8);
   L.off_tl = o; o = al(o + (size_t)p.off.n * 8);
   L.off_tx = o; o = al(o + (size_t)p.off.n * 8);
@@ -386,6 +409,7 @@ inline PackedLayout make_packed_layout(const MatvecProblem& p) {
   L.off_dr = o; o = al(o + (size_t)p.diag.n * 8);
   L.off_ds = o; o = al(o + (size_t)p.diag.n * 8);
   L.off_dv = o; o = al(o + (size_t)p.diag.n * 16);
+  L.off_sectors = o; o = al(o + (size_t)n_sectors * sizeof(SectorDesc));
   L.total = o;
   return L;
 }
@@ -396,15 +420,24 @@ __device__ __forceinline__ uint64_t flip_packed(uint64_t cand, uint64_t flipkey)
   return cand ^ (flipkey & (((uint64_t)m << 32) | m));
 }
 
-template <int GPL, bool INV, bool CPLX, int K>
-__global__ void __launch_bounds__(320, 2)
-    k_matvec_packed(const MatvecProblem p, const PackedLayout L, const double* __restrict__ x, int64_t ldx,
-                    double* __restrict__ y, int64_t ldy, int* __restrict__ err,
-                    const uint64_t* __restrict__ binom) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  constexpr unsigned FULL = 0xffffffffu;
-  constexpr int Gp = 32 * GPL;
-  constexpr int Q = 32 / K;
+// Shared-memory tables of the packed kernels.
+struct PackedTables {
+  const uint64_t* oh;  // one-hot site images [n_bits][gpl * 32]
+  const double2* ch;   // characters (single-sector kernel only)
+  const uint64_t *tm, *tl, *tx, *ts;
+  const double2* tv;
+  const uint32_t* ti;
+  const uint64_t *dm, *dr, *ds;
+  const double2* dv;
+  int nt, nd;
+};
+
+// Copies the group's site images, the term tables and (with_chars) the characters into shared
+// memory; the caller synchronises the block afterwards.
+__device__ __forceinline__ PackedTables stage_packed(const MatvecProblem& p, const PackedLayout& L,
+                                                     unsigned char* smem, bool with_chars) {
+  PackedTables T;
+  const int Gp = 32 * p.group.gpl;
   uint64_t* oh = (uint64_t*)(smem + L.off_onehot);
   double2* ch = (double2*)(smem + L.off_chars);
   uint64_t* tm = (uint64_t*)(smem + L.off_tm);
@@ -417,9 +450,8 @@ __global__ void __launch_bounds__(320, 2)
   uint64_t* dr = (uint64_t*)(smem + L.off_dr);
   uint64_t* ds = (uint64_t*)(smem + L.off_ds);
   double2* dv = (double2*)(smem + L.off_dv);
-  const int nbits = p.group.n_bits;
-  stage_u64(oh, p.group.onehot_packed, nbits * Gp);
-  stage_d2(ch, p.group.chars_packed, Gp);
+  stage_u64(oh, p.group.onehot_packed, p.group.n_bits * Gp);
+  if (with_chars) stage_d2(ch, p.group.chars_packed, Gp);
   stage_u64(tm, p.off.m, p.off.n);
   stage_u64(tl, p.off.l, p.off.n);
   stage_u64(tx, p.off.x, p.off.n);
@@ -430,173 +462,245 @@ __global__ void __launch_bounds__(320, 2)
   stage_u64(dr, p.diag.r, p.diag.n);
   stage_u64(ds, p.diag.s, p.diag.n);
   stage_d2(dv, p.diag.v, p.diag.n);
-  __syncthreads();
+  T.oh = oh; T.ch = ch; T.tm = tm; T.tl = tl; T.tx = tx; T.ts = ts; T.tv = tv; T.ti = ti;
+  T.dm = dm; T.dr = dr; T.ds = ds; T.dv = dv;
+  T.nt = p.off.n;
+  T.nd = p.diag.n;
+  return T;
+}
 
+// One output row of the packed kernels (executed by a whole warp): y[row, 0..K) for the sector
+// described by (ix, chars, spin_inversion, x, y).
+template <int GPL, bool INV, bool CPLX, int K>
+__device__ __forceinline__ void packed_row(const PackedTables& T, const int nbits, const DeviceIndex& ix,
+                                           const double2* __restrict__ chars, const int spin_inversion,
+                                           const DeviceConstraint& cons, const double* __restrict__ x,
+                                           const int64_t ldx, double* __restrict__ y, const int64_t ldy,
+                                           const int64_t row, int* __restrict__ err,
+                                           const uint64_t* __restrict__ binom,
+                                           unsigned long long* nnz_counter) {
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int Gp = 32 * GPL;
+  constexpr int Q = 32 / K;
   const int lane = threadIdx.x & 31;
   const int SH = 64 - nbits;
-  const uint64_t flipkey = (p.group.flip << SH) | 1ull;
   const uint64_t lowmask = (1ull << SH) - 1;
+  const uint64_t flipkey = ((~0ull >> SH) << SH) | 1ull;  // all state bits and the flip bit
   const int rhs = lane % K;
   const int q = lane / K;
-  const uint64_t* ohl = oh + lane;
+  const uint64_t* ohl = T.oh + lane;
+  const int nt = T.nt;
+
+  const uint64_t a = __ldg(ix.reps + row);
+  const double na = __ldg(ix.norms + row);
+  if (na == 0.0) {
+    // A representative whose orbit norm is zero spans no state of the sector (the reference's
+    // floating stabiliser sum can keep such states as rounding residue in complex sectors): its
+    // row and column of H are zero.  `na` is the same on every lane, so the warp stays converged.
+    if (lane < K) {
+      if constexpr (CPLX) reinterpret_cast<double2*>(y)[row * ldy + lane] = make_double2(0.0, 0.0);
+      else y[row * ldy + lane] = 0.0;
+    }
+    return;
+  }
+  uint64_t ga[GPL];
+#pragma unroll
+  for (int k = 0; k < GPL; ++k) ga[k] = 0;
+  for (uint64_t bits = a; bits != 0; bits &= bits - 1) {
+    const uint64_t* r = ohl + (__ffsll((long long)bits) - 1) * Gp;
+#pragma unroll
+    for (int k = 0; k < GPL; ++k) ga[k] ^= r[32 * k];
+  }
+#pragma unroll
+  for (int k = 0; k < GPL; ++k) ga[k] |= (uint64_t)(2 * (lane + 32 * k));
+
+  double dre = 0.0, dim = 0.0;
+  for (int t = lane; t < T.nd; t += 32) {
+    if ((a & T.dm[t]) == T.dr[t]) {
+      const double2 v = T.dv[t];
+      const bool neg = __popcll(a & T.ds[t]) & 1;
+      dre += neg ? -v.x : v.x;
+      if constexpr (CPLX) dim += neg ? -v.y : v.y;
+    }
+  }
+  dre = warp_sum(dre);
+  if constexpr (CPLX) dim = warp_sum(dim);
+
+  Acc acc;
+  unsigned found = 0;
+  uint64_t my_key = ~0ull;
+  double2 my_c = make_double2(0.0, 0.0);
+  int nslot = 0;
+
+  auto flush = [&]() {
+    int64_t j = -1;
+    double fre = 0.0, fim = 0.0;
+    if (lane < nslot) {
+      const uint64_t rep = my_key >> SH;
+      const uint32_t idx = (uint32_t)(my_key & lowmask);
+      j = mv_index_lookup(ix, rep, binom);
+      const double nj = j >= 0 ? __ldg(ix.norms + j) : 0.0;
+      if (nj == 0.0) j = -1;  // zero-norm column
+      found += (j >= 0);
+      if (j >= 0) {
+        double2 chi = chars[idx >> 1];
+        if (INV && (idx & 1) && spin_inversion == -1) chi = make_double2(-chi.x, -chi.y);
+        const C2 f = cmul_conj_b(C2{my_c.x, my_c.y}, C2{chi.x, chi.y});
+        fre = f.re * nj;
+        fim = f.im * nj;
+      }
+    }
+    for (int s0 = 0; s0 < nslot; s0 += Q) {
+      const int s = s0 + q;
+      const int src = s & 31;
+      const int64_t js = (K == 1) ? j : __shfl_sync(FULL, j, src);
+      const double sre = (K == 1) ? fre : __shfl_sync(FULL, fre, src);
+      const double sim = (K == 1) ? fim : __shfl_sync(FULL, fim, src);
+      if (s < nslot && js >= 0) {
+        if constexpr (CPLX) {
+          const double2 xv = __ldg(reinterpret_cast<const double2*>(x) + js * ldx + rhs);
+          acc.re += sre * xv.x - sim * xv.y;
+          acc.im += sre * xv.y + sim * xv.x;
+        } else {
+          acc.re += sre * __ldg(x + js * ldx + rhs);
+        }
+      }
+      if (K == 1) break;
+    }
+  };
+
+  for (int t0 = 0; t0 < nt; t0 += 32) {
+    const int tt = t0 + lane;
+    const bool hit = tt < nt && (a & T.tm[tt]) == T.tl[tt];
+    unsigned mask = __ballot_sync(FULL, hit);
+    while (mask != 0) {
+      const int t = t0 + __ffs(mask) - 1;
+      mask &= mask - 1;
+      const uint64_t xt = T.tx[t];
+      const uint32_t info = T.ti[t];
+      const uint64_t beta = a ^ xt;
+      if (info & kTermNeedsCheck) {
+        if (!constraint_ok(cons, beta)) {
+          if (lane == 0) atomicOr(err, 1);
+          continue;
+        }
+      }
+      // coefficient sign (-1)^popcount(beta & s) applied to the sign bits (integer ops)
+      double2 c = T.tv[t];
+      {
+        const long long sbit = (long long)(__popcll(beta & T.ts[t]) & 1) << 63;
+        c.x = __longlong_as_double(__double_as_longlong(c.x) ^ sbit);
+        c.y = __longlong_as_double(__double_as_longlong(c.y) ^ sbit);
+      }
+      uint64_t cand[GPL];
+      if (((info >> 16) & 0xffu) == 2u) {
+        const uint64_t* r0 = ohl + (int)(info & 0xffu) * Gp;
+        const uint64_t* r1 = ohl + (int)((info >> 8) & 0xffu) * Gp;
+#pragma unroll
+        for (int k = 0; k < GPL; ++k) {
+          cand[k] = ga[k] ^ r0[32 * k] ^ r1[32 * k];
+          if (INV) cand[k] = flip_packed(cand[k], flipkey);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < GPL; ++k) {
+          uint64_t v = ga[k];
+          for (uint64_t bits = xt; bits != 0; bits &= bits - 1)
+            v ^= ohl[(__ffsll((long long)bits) - 1) * Gp + 32 * k];
+          cand[k] = INV ? flip_packed(v, flipkey) : v;
+        }
+      }
+      // pairwise (tree) minimum: short dependency chains
+#pragma unroll
+      for (int w = 1; w < GPL; w *= 2) {
+#pragma unroll
+        for (int k = 0; k + w < GPL; k += 2 * w) cand[k] = cand[k + w] < cand[k] ? cand[k + w] : cand[k];
+      }
+      const uint64_t best = cand[0];
+      const uint32_t hi = (uint32_t)(best >> 32), lo = (uint32_t)best;
+      const uint32_t mhi = __reduce_min_sync(FULL, hi);
+      const uint32_t mlo = __reduce_min_sync(FULL, hi == mhi ? lo : 0xffffffffu);
+      if (lane == nslot) {
+        my_key = ((uint64_t)mhi << 32) | mlo;
+        my_c = c;
+      }
+      if (++nslot == 32) {
+        flush();
+        nslot = 0;
+      }
+    }
+  }
+  if (nslot > 0) flush();
+  if (nnz_counter != nullptr) {
+    const unsigned total = __reduce_add_sync(FULL, found);
+    if (lane == 0 && total) atomicAdd(nnz_counter, (unsigned long long)total);
+  }
+
+  const double inv_na = 1.0 / na;
+  if constexpr (CPLX) {
+#pragma unroll
+    for (int d = 16; d >= K; d >>= 1) {
+      acc.re += __shfl_xor_sync(FULL, acc.re, d);
+      acc.im += __shfl_xor_sync(FULL, acc.im, d);
+    }
+    if (lane < K) {
+      const double2 xi = __ldg(reinterpret_cast<const double2*>(x) + row * ldx + lane);
+      double2 out;
+      out.x = acc.re * inv_na + (dre * xi.x - dim * xi.y);
+      out.y = acc.im * inv_na + (dre * xi.y + dim * xi.x);
+      reinterpret_cast<double2*>(y)[row * ldy + lane] = out;
+    }
+  } else {
+#pragma unroll
+    for (int d = 16; d >= K; d >>= 1) acc.re += __shfl_xor_sync(FULL, acc.re, d);
+    if (lane < K) y[row * ldy + lane] = acc.re * inv_na + dre * __ldg(x + row * ldx + lane);
+  }
+}
+
+template <int GPL, bool INV, bool CPLX, int K>
+__global__ void __launch_bounds__(320, 2)
+    k_matvec_packed(const MatvecProblem p, const PackedLayout L, const double* __restrict__ x, int64_t ldx,
+                    double* __restrict__ y, int64_t ldy, int* __restrict__ err,
+                    const uint64_t* __restrict__ binom) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const PackedTables T = stage_packed(p, L, smem, true);
+  __syncthreads();
   const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int nt = p.off.n;
+  for (int64_t row = warp_id; row < p.n_rows; row += n_warps)
+    packed_row<GPL, INV, CPLX, K>(T, p.group.n_bits, p.index, T.ch, p.group.spin_inversion, p.constraint, x, ldx,
+                                  y, ldy, row, err, binom, p.nnz_counter);
+}
 
-  for (int64_t row = warp_id; row < p.n_rows; row += n_warps) {
-    const uint64_t a = __ldg(p.index.reps + row);
-    const double na = __ldg(p.index.norms + row);
-    uint64_t ga[GPL];
-#pragma unroll
-    for (int k = 0; k < GPL; ++k) ga[k] = 0;
-    for (uint64_t bits = a; bits != 0; bits &= bits - 1) {
-      const uint64_t* r = ohl + (__ffsll((long long)bits) - 1) * Gp;
-#pragma unroll
-      for (int k = 0; k < GPL; ++k) ga[k] ^= r[32 * k];
+// Batched kernel: the rows of all sectors form one row space that a persistent grid walks; each
+// warp looks up the sector of its row in the shared sector table.  `p` carries the shared
+// tables (site images, terms, constraint) of the first sector.
+template <int GPL, bool INV, int K>
+__global__ void __launch_bounds__(320, 2)
+    k_matvec_sectors(const MatvecProblem p, const PackedLayout L, const SectorDesc* __restrict__ sectors,
+                     int n_sectors, int64_t total_rows, int64_t ldx, int64_t ldy, int* __restrict__ err,
+                     const uint64_t* __restrict__ binom) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const PackedTables T = stage_packed(p, L, smem, false);
+  SectorDesc* sd = (SectorDesc*)(smem + L.off_sectors);
+  {
+    const uint64_t* src = reinterpret_cast<const uint64_t*>(sectors);
+    uint64_t* dst = reinterpret_cast<uint64_t*>(sd);
+    const int words = n_sectors * (int)(sizeof(SectorDesc) / 8);
+    for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t row = warp_id; row < total_rows; row += n_warps) {
+    int lo = 0, hi = n_sectors - 1;  // last sector with row_begin <= row
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (sd[mid].row_begin <= row) lo = mid; else hi = mid - 1;
     }
-#pragma unroll
-    for (int k = 0; k < GPL; ++k) ga[k] |= (uint64_t)(2 * (lane + 32 * k));
-
-    double dre = 0.0, dim = 0.0;
-    for (int t = lane; t < p.diag.n; t += 32) {
-      if ((a & dm[t]) == dr[t]) {
-        const double2 v = dv[t];
-        const bool neg = __popcll(a & ds[t]) & 1;
-        dre += neg ? -v.x : v.x;
-        if constexpr (CPLX) dim += neg ? -v.y : v.y;
-      }
-    }
-    dre = warp_sum(dre);
-    if constexpr (CPLX) dim = warp_sum(dim);
-
-    Acc acc;
-    unsigned found = 0;
-    uint64_t my_key = ~0ull;
-    double2 my_c = make_double2(0.0, 0.0);
-    int nslot = 0;
-
-    auto flush = [&]() {
-      int64_t j = -1;
-      double fre = 0.0, fim = 0.0;
-      if (lane < nslot) {
-        const uint64_t rep = my_key >> SH;
-        const uint32_t idx = (uint32_t)(my_key & lowmask);
-        j = mv_index_lookup(p.index, rep, binom);
-        found += (j >= 0);
-        if (j >= 0) {
-          double2 chi = ch[idx >> 1];
-          if (INV && (idx & 1) && p.group.spin_inversion == -1) chi = make_double2(-chi.x, -chi.y);
-          const double nj = __ldg(p.index.norms + j);
-          const C2 f = cmul_conj_b(C2{my_c.x, my_c.y}, C2{chi.x, chi.y});
-          fre = f.re * nj;
-          fim = f.im * nj;
-        }
-      }
-      for (int s0 = 0; s0 < nslot; s0 += Q) {
-        const int s = s0 + q;
-        const int src = s & 31;
-        const int64_t js = (K == 1) ? j : __shfl_sync(FULL, j, src);
-        const double sre = (K == 1) ? fre : __shfl_sync(FULL, fre, src);
-        const double sim = (K == 1) ? fim : __shfl_sync(FULL, fim, src);
-        if (s < nslot && js >= 0) {
-          if constexpr (CPLX) {
-            const double2 xv = __ldg(reinterpret_cast<const double2*>(x) + js * ldx + rhs);
-            acc.re += sre * xv.x - sim * xv.y;
-            acc.im += sre * xv.y + sim * xv.x;
-          } else {
-            acc.re += sre * __ldg(x + js * ldx + rhs);
-          }
-        }
-        if (K == 1) break;
-      }
-    };
-
-    for (int t0 = 0; t0 < nt; t0 += 32) {
-      const int tt = t0 + lane;
-      const bool hit = tt < nt && (a & tm[tt]) == tl[tt];
-      unsigned mask = __ballot_sync(FULL, hit);
-      while (mask != 0) {
-        const int t = t0 + __ffs(mask) - 1;
-        mask &= mask - 1;
-        const uint64_t xt = tx[t];
-        const uint32_t info = ti[t];
-        const uint64_t beta = a ^ xt;
-        if (info & kTermNeedsCheck) {
-          if (!constraint_ok(p.constraint, beta)) {
-            if (lane == 0) atomicOr(err, 1);
-            continue;
-          }
-        }
-        // coefficient sign (-1)^popcount(beta & s) applied to the sign bits (integer ops)
-        double2 c = tv[t];
-        {
-          const long long sbit = (long long)(__popcll(beta & ts[t]) & 1) << 63;
-          c.x = __longlong_as_double(__double_as_longlong(c.x) ^ sbit);
-          c.y = __longlong_as_double(__double_as_longlong(c.y) ^ sbit);
-        }
-        uint64_t cand[GPL];
-        if (((info >> 16) & 0xffu) == 2u) {
-          const uint64_t* r0 = ohl + (int)(info & 0xffu) * Gp;
-          const uint64_t* r1 = ohl + (int)((info >> 8) & 0xffu) * Gp;
-#pragma unroll
-          for (int k = 0; k < GPL; ++k) {
-            cand[k] = ga[k] ^ r0[32 * k] ^ r1[32 * k];
-            if (INV) cand[k] = flip_packed(cand[k], flipkey);
-          }
-        } else {
-#pragma unroll
-          for (int k = 0; k < GPL; ++k) {
-            uint64_t v = ga[k];
-            for (uint64_t bits = xt; bits != 0; bits &= bits - 1)
-              v ^= ohl[(__ffsll((long long)bits) - 1) * Gp + 32 * k];
-            cand[k] = INV ? flip_packed(v, flipkey) : v;
-          }
-        }
-        // pairwise (tree) minimum: short dependency chains
-#pragma unroll
-        for (int w = 1; w < GPL; w *= 2) {
-#pragma unroll
-          for (int k = 0; k + w < GPL; k += 2 * w) cand[k] = cand[k + w] < cand[k] ? cand[k + w] : cand[k];
-        }
-        const uint64_t best = cand[0];
-        const uint32_t hi = (uint32_t)(best >> 32), lo = (uint32_t)best;
-        const uint32_t mhi = __reduce_min_sync(FULL, hi);
-        const uint32_t mlo = __reduce_min_sync(FULL, hi == mhi ? lo : 0xffffffffu);
-        if (lane == nslot) {
-          my_key = ((uint64_t)mhi << 32) | mlo;
-          my_c = c;
-        }
-        if (++nslot == 32) {
-          flush();
-          nslot = 0;
-        }
-      }
-    }
-    if (nslot > 0) flush();
-    if (p.nnz_counter != nullptr) {
-      const unsigned total = __reduce_add_sync(FULL, found);
-      if (lane == 0 && total) atomicAdd(p.nnz_counter, (unsigned long long)total);
-    }
-
-    const double inv_na = 1.0 / na;
-    if constexpr (CPLX) {
-#pragma unroll
-      for (int d = 16; d >= K; d >>= 1) {
-        acc.re += __shfl_xor_sync(FULL, acc.re, d);
-        acc.im += __shfl_xor_sync(FULL, acc.im, d);
-      }
-      if (lane < K) {
-        const double2 xi = __ldg(reinterpret_cast<const double2*>(x) + row * ldx + lane);
-        double2 out;
-        out.x = acc.re * inv_na + (dre * xi.x - dim * xi.y);
-        out.y = acc.im * inv_na + (dre * xi.y + dim * xi.x);
-        reinterpret_cast<double2*>(y)[row * ldy + lane] = out;
-      }
-    } else {
-#pragma unroll
-      for (int d = 16; d >= K; d >>= 1) acc.re += __shfl_xor_sync(FULL, acc.re, d);
-      if (lane < K) y[row * ldy + lane] = acc.re * inv_na + dre * __ldg(x + row * ldx + lane);
-    }
+    const SectorDesc& S = sd[lo];
+    packed_row<GPL, INV, true, K>(T, p.group.n_bits, S.index, S.chars, (int)S.spin_inversion, p.constraint, S.x,
+                                  ldx, S.y, ldy, row - S.row_begin, err, binom, p.nnz_counter);
   }
 }
 

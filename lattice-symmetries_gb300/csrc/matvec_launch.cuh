@@ -1,19 +1,36 @@
 // matvec_launch.cuh -- launch helpers shared by the matvec translation units.
 #pragma once
+#include <array>
 #include <type_traits>
+#include <unordered_map>
 
 #include "matvec_dispatch.h"
 #include "matvec_impl.cuh"
 
 namespace lsg {
 
+// Raises a kernel's dynamic shared-memory limit once per (kernel, device, size): later launches,
+// including ones recorded in a CUDA graph, make no attribute call.  Callers hold the library lock.
+inline bool ensure_smem_limit(const void* kern, size_t bytes) {
+  static std::unordered_map<const void*, std::array<int, 64>> set_bytes;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  auto it = set_bytes.find(kern);
+  if (it != set_bytes.end() && it->second[dev] >= (int)bytes) return true;
+  if (!cuda_ok(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes),
+               "smem attribute"))
+    return false;
+  if (it == set_bytes.end()) it = set_bytes.emplace(kern, std::array<int, 64>{}).first;
+  it->second[dev] = (int)bytes;
+  return true;
+}
+
 template <typename Kernel, typename Layout>
 static int launch_with_smem(Kernel kern, const char* name, const MatvecProblem& p, const Layout& L,
                             LaunchShape sh, const double* x, int64_t ldx, double* y, int64_t ldy, int* err,
                             const uint64_t* binom, cudaStream_t s) {
-  if (!cuda_ok(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total),
-               "smem attribute"))
-    return LS_GPU_ERR_CUDA;
+  if (!ensure_smem_limit((const void*)kern, L.total)) return LS_GPU_ERR_CUDA;
   kern<<<sh.blocks, sh.threads, L.total, s>>>(p, L, x, ldx, y, ldy, err, binom);
   return cuda_ok(cudaGetLastError(), name) ? 0 : LS_GPU_ERR_CUDA;
 }

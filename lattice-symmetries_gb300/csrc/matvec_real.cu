@@ -13,9 +13,7 @@ static int run_plain(const MatvecProblem& p, const SmemLayout& L, LaunchShape sh
                      int64_t ldx, double* y, int64_t ldy, int k, int* err, const uint64_t* binom,
                      cudaStream_t s) {
   auto kern = k_matvec_plain<CPLX, INV>;
-  if (!cuda_ok(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total),
-               "smem attribute"))
-    return LS_GPU_ERR_CUDA;
+  if (!ensure_smem_limit((const void*)kern, L.total)) return LS_GPU_ERR_CUDA;
   kern<<<sh.blocks, sh.threads, L.total, s>>>(p, L, x, ldx, y, ldy, k, err, binom);
   return cuda_ok(cudaGetLastError(), "k_matvec_plain") ? 0 : LS_GPU_ERR_CUDA;
 }

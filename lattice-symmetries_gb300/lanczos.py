@@ -1,0 +1,162 @@
+"""Block Lanczos on the GPU for many symmetry sectors at once.
+
+This replaces the eigensolver drivers that sit on top of the reference's matvec (scipy's eigsh
+over Operator._matvec in python/lattice_symmetries/__init__.py:751-752, and the PRIMME driver of
+chapel/src/Diagonalize.chpl): every step applies H to a block of k vectors in every sector with
+ONE batched matvec (SectorBatch), then orthogonalises all sectors together with batched dense
+algebra.  One step (matvec + orthogonalisation) is recorded in a CUDA graph and replayed.
+
+Recurrence (per sector, blocks of k columns, Q_0 orthonormal, Q_{-1} = 0, B_{-1} = 0):
+
+    W   = H Q_j
+    A_j = Q_j^H W
+    W  <- W - Q_j A_j - Q_{j-1} B_{j-1}^H        (+ one local re-orthogonalisation against Q_j)
+    W   = Q_{j+1} B_j                             (Cholesky QR, two passes)
+
+and the eigenvalues of the block-tridiagonal T (diagonal blocks A_j, sub-diagonal blocks B_j)
+approximate the extremal eigenvalues of H.  There is no global re-orthogonalisation, so converged
+Ritz values can repeat ("ghosts"); the lowest ones are reliable.
+"""
+
+from __future__ import annotations
+
+from typing import Callable, List, Optional, Tuple
+
+import numpy as np
+
+
+def _cholqr(W, eps: float = 1e-15):
+    """W = Q R with Q orthonormal (batched over the leading dimension): two Cholesky-QR passes.
+    A tiny diagonal shift keeps exhausted blocks (W ~ 0) finite instead of NaN."""
+    import torch
+
+    k = W.shape[-1]
+    eye = torch.eye(k, dtype=W.dtype, device=W.device)
+    R = None
+    Q = W
+    for _ in range(2):
+        G = Q.mH @ Q
+        G = 0.5 * (G + G.mH)
+        scale = torch.diagonal(G, dim1=-2, dim2=-1).real.mean(-1).clamp_min(1e-300)
+        G = G + (eps * scale)[..., None, None] * eye
+        L, _ = torch.linalg.cholesky_ex(G)
+        Rp = L.mH
+        Q = torch.linalg.solve_triangular(Rp, Q, upper=True, left=False)
+        R = Rp if R is None else Rp @ R
+    return Q, R
+
+
+def lanczos_step(apply: Callable[[], None], Q, W, Qp, Bp, A_out, B_out) -> None:
+    """One block-Lanczos step on preallocated tensors ([S, D, k] blocks, [S, k, k] coefficients).
+
+    `apply()` must compute W = H Q in place.  On return Q holds Q_{j+1}, Qp holds Q_j,
+    Bp = B_out = B_j and A_out = A_j.  Everything is stream-ordered (no host synchronisation), so
+    the step can be captured in a CUDA graph."""
+    apply()
+    A = Q.mH @ W
+    W.sub_(Q @ A)
+    W.sub_(Qp @ Bp.mH)
+    C = Q.mH @ W  # local re-orthogonalisation against the current block
+    W.sub_(Q @ C)
+    A = A + C
+    A = 0.5 * (A + A.mH)
+    Qn, B = _cholqr(W)
+    Qp.copy_(Q)
+    Q.copy_(Qn)
+    Bp.copy_(B)
+    A_out.copy_(A)
+    B_out.copy_(B)
+
+
+def block_tridiagonal(A: List, B: List):
+    """Assembles T [S, n k, n k] from A_0..A_{n-1} and B_0..B_{n-2} ([S, k, k] each)."""
+    import torch
+
+    n = len(A)
+    S, k, _ = A[0].shape
+    T = torch.zeros((S, n * k, n * k), dtype=A[0].dtype, device=A[0].device)
+    for j in range(n):
+        T[:, j * k:(j + 1) * k, j * k:(j + 1) * k] = A[j]
+        if j + 1 < n:
+            T[:, (j + 1) * k:(j + 2) * k, j * k:(j + 1) * k] = B[j]
+            T[:, j * k:(j + 1) * k, (j + 1) * k:(j + 2) * k] = B[j].mH
+    return T
+
+
+def block_lanczos(apply: Callable[[], None], Q, W, steps: int, graph: bool = False,
+                  timer: Optional[dict] = None):
+    """Runs `steps` block-Lanczos steps with W = H Q computed by `apply()`; Q must hold an
+    orthonormal starting block.  Returns the eigenvalues of T per sector ([S, steps * k],
+    ascending).  With graph=True one step is captured in a CUDA graph after a warm-up step
+    (which is itself step 0) and replayed for the rest."""
+    import torch
+
+    S, D, k = Q.shape
+    Qp = torch.zeros_like(Q)
+    Bp = torch.zeros((S, k, k), dtype=Q.dtype, device=Q.device)
+    A_cur = torch.zeros_like(Bp)
+    B_cur = torch.zeros_like(Bp)
+    A_hist, B_hist = [], []
+
+    def record():
+        A_hist.append(A_cur.clone())
+        B_hist.append(B_cur.clone())
+
+    use_graph = graph and Q.is_cuda
+    g = None
+    if use_graph:
+        side = torch.cuda.Stream(Q.device)
+        side.wait_stream(torch.cuda.current_stream(Q.device))
+        with torch.cuda.stream(side):
+            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur)  # step 0, also the warm-up
+        torch.cuda.current_stream(Q.device).wait_stream(side)
+        record()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur)
+        # capture does not execute: step 1 runs at the first replay below
+    start = end = None
+    if timer is not None and Q.is_cuda:
+        torch.cuda.synchronize(Q.device)
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record()
+    j0 = len(A_hist)
+    for _ in range(j0, steps):
+        if g is not None:
+            g.replay()
+        else:
+            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur)
+        record()
+    if start is not None:
+        end.record()
+        torch.cuda.synchronize(Q.device)
+        timer["ms"] = start.elapsed_time(end)
+        timer["steps"] = steps - j0
+    T = block_tridiagonal(A_hist, B_hist)
+    return torch.linalg.eigvalsh(T)
+
+
+def random_start(batch, seed: int = 0):
+    """Fills batch.X with an orthonormal random block per sector (zero padding rows)."""
+    import torch
+
+    gen = torch.Generator(device="cpu").manual_seed(seed)
+    for s in range(batch.number_sectors):
+        d = batch.sizes[s]
+        x = torch.randn((d, batch.k), dtype=torch.float64, generator=gen) + \
+            1j * torch.randn((d, batch.k), dtype=torch.float64, generator=gen)
+        batch.X[s].zero_()
+        batch.X[s, :d].copy_(x.to(torch.complex128))
+    Q, _ = _cholqr(batch.X)
+    batch.X.copy_(Q)
+    return batch.X
+
+
+def sector_ground_states(batch, steps: int, seed: int = 0, graph: bool = True,
+                         timer: Optional[dict] = None) -> np.ndarray:
+    """Lowest eigenvalue of every sector of a SectorBatch after `steps` block-Lanczos steps."""
+    random_start(batch, seed)
+    ev = block_lanczos(lambda: batch.run(), batch.X, batch.Y, steps, graph=graph, timer=timer)
+    batch.check_errors()
+    return ev[:, 0].cpu().numpy()

@@ -538,6 +538,9 @@ int lso_matvec(const lso_group *g, const lso_projection *pr, int64_t D, const ui
     for (int64_t i = row_begin; i < row_end; ++i) {
       const uint64_t a = reps[i];
       double accr = 0.0, acci = 0.0;
+      /* A representative whose norm is zero spans no state of the sector: its row and column
+       * of H are zero (the reference divides by such norms; see the matvec kernels). */
+      if (pr->projection == 2 && rep_norms[i] == 0.0) continue;
       for (int t = 0; t < diag->n; ++t) {
         if ((a & diag->m[t]) == diag->r[t]) {
           int sign = 1 - 2 * (__builtin_popcountll(a & diag->s[t]) % 2);
@@ -559,6 +562,7 @@ int lso_matvec(const lso_group *g, const lso_projection *pr, int64_t D, const ui
     for (int64_t j = row_begin; j < row_end; ++j) {
       const uint64_t a = reps[j];
       const double na = pr->projection == 2 ? rep_norms[j] : 1.0;
+      if (na == 0.0) continue; /* zero-norm representative: zero column */
       for (int t = 0; t < off->n; ++t) {
         if ((a & off->m[t]) != off->r[t]) continue;
         const int sign = 1 - 2 * (__builtin_popcountll(a & off->s[t]) % 2);
