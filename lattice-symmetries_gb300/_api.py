@@ -630,7 +630,7 @@ class SectorBatch:
     Hamiltonian in all momentum / spin-inversion sectors of one group).  The batch owns two
     zero-padded complex128 tensors ``X`` and ``Y`` of shape [n_sectors, D_max, k]; sector s uses
     the rows [0, D_s) of ``X[s]`` and ``Y[s]`` (``x(s)``, ``y(s)`` are those views) and padding rows
-    stay zero.  ``run()`` computes Y = H X (or H^dagger X) with one persistent kernel launch per
+    stay zero (D_max is rounded up to a multiple of 256).  ``run()`` computes Y = H X (or H^dagger X) with one persistent kernel launch per
     chunk of up to 16 right-hand sides over the rows of all sectors (``batched`` says whether the
     sectors could share one launch); ``capture()`` records that launch in a CUDA graph and
     ``replay()`` re-launches it.  No reference counterpart: the reference applies one operator to
@@ -650,7 +650,7 @@ class SectorBatch:
         self.adjoint = bool(adjoint)
         self.sizes = [op.basis.number_states for op in operators]
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
-        d_max = max(max(self.sizes), 1)
+        d_max = (max(max(self.sizes), 1) + 255) // 256 * 256  # row blocks of 256 for Gram products
         self.X = torch.zeros((len(operators), d_max, self.k), dtype=torch.complex128, device=self.device)
         self.Y = torch.zeros_like(self.X)
         n = len(operators)

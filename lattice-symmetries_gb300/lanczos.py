@@ -25,9 +25,32 @@ from typing import Callable, List, Optional, Tuple
 import numpy as np
 
 
+def _row_chunks(D: int) -> int:
+    """Largest power of two c <= 256 with D % c == 0 and D / c >= 64: the row blocks of a Gram
+    product, so that the reduction over D runs as c independent GEMMs per sector."""
+    c = 1
+    while c < 256 and D % (2 * c) == 0 and D // (2 * c) >= 64:
+        c *= 2
+    return c
+
+
+def _gram(X, Y):
+    """X^H Y for [S, D, k] blocks as [S, k, k].  A single GEMM with inner dimension D (hundreds of
+    thousands) and a 16 x 16 output leaves most of the GPU idle; splitting D into row blocks gives
+    S * c GEMMs whose partial results are summed."""
+    S, D, k = X.shape
+    c = _row_chunks(D)
+    if c == 1:
+        return X.mH @ Y
+    Xc = X.reshape(S, c, D // c, k)
+    Yc = Y.reshape(S, c, D // c, k)
+    return (Xc.mH @ Yc).sum(1)
+
+
 def _cholqr(W, eps: float = 1e-15):
     """W = Q R with Q orthonormal (batched over the leading dimension): two Cholesky-QR passes.
-    A tiny diagonal shift keeps exhausted blocks (W ~ 0) finite instead of NaN."""
+    A tiny diagonal shift keeps exhausted blocks (W ~ 0) finite instead of NaN.  The k x k factor
+    is inverted explicitly, so that applying it is a GEMM rather than a triangular solve over D."""
     import torch
 
     k = W.shape[-1]
@@ -35,13 +58,14 @@ def _cholqr(W, eps: float = 1e-15):
     R = None
     Q = W
     for _ in range(2):
-        G = Q.mH @ Q
+        G = _gram(Q, Q)
         G = 0.5 * (G + G.mH)
         scale = torch.diagonal(G, dim1=-2, dim2=-1).real.mean(-1).clamp_min(1e-300)
         G = G + (eps * scale)[..., None, None] * eye
         L, _ = torch.linalg.cholesky_ex(G)
         Rp = L.mH
-        Q = torch.linalg.solve_triangular(Rp, Q, upper=True, left=False)
+        Rinv = torch.linalg.solve_triangular(Rp, eye.expand_as(Rp), upper=True)
+        Q = Q @ Rinv
         R = Rp if R is None else Rp @ R
     return Q, R
 
@@ -52,12 +76,14 @@ def lanczos_step(apply: Callable[[], None], Q, W, Qp, Bp, A_out, B_out) -> None:
     `apply()` must compute W = H Q in place.  On return Q holds Q_{j+1}, Qp holds Q_j,
     Bp = B_out = B_j and A_out = A_j.  Everything is stream-ordered (no host synchronisation), so
     the step can be captured in a CUDA graph."""
+    import torch
+
     apply()
-    A = Q.mH @ W
-    W.sub_(Q @ A)
-    W.sub_(Qp @ Bp.mH)
-    C = Q.mH @ W  # local re-orthogonalisation against the current block
-    W.sub_(Q @ C)
+    A = _gram(Q, W)
+    W.baddbmm_(Q, A, beta=1.0, alpha=-1.0)
+    W.baddbmm_(Qp, Bp.mH, beta=1.0, alpha=-1.0)
+    C = _gram(Q, W)  # local re-orthogonalisation against the current block
+    W.baddbmm_(Q, C, beta=1.0, alpha=-1.0)
     A = A + C
     A = 0.5 * (A + A.mH)
     Qn, B = _cholqr(W)
