@@ -290,10 +290,14 @@ int ls_gpu_check_errors(void *stream);
 /* Number of off-diagonal matrix elements (generated targets found in the basis) of H. */
 int ls_gpu_count_nonzeros(ls_hs_operator const *op, int64_t *nnz);
 
-/* Per-coupling inner products out[c] = <g, H_c x> for an operator whose terms are tagged with
- * coupling ids (term_coupling[t] in [0, n_couplings) for the off-diagonal terms, then the
- * diagonal terms, in table order).  g, x: complex128 [D]; out: complex128 [n_couplings]
- * (device). */
+/* Per-coupling inner products out[c] = <g, H_c x> = sum_i conj(g_i) (H_c x)_i for an operator
+ * H = sum_c H_c whose terms are tagged with coupling ids: term_coupling[t] in [0, n_couplings) for
+ * the off-diagonal terms, then the diagonal terms, in table order (host array).  g, x: complex128
+ * [D]; out: complex128 [n_couplings]; all device pointers, stream-ordered.  This is the gradient
+ * of Re<g, H(theta) x> with respect to the couplings theta (Re out[c]).  One fused pass (the
+ * packed orbit scan) for bases with lattice symmetries of at most 128 elements and at most 4
+ * couplings; other operators return LS_GPU_ERR_INVALID (use one matvec per coupling).  No
+ * counterpart in the reference. */
 int ls_gpu_coupling_inner_products(ls_hs_operator const *op, int n_couplings,
                                    int32_t const *term_coupling, double const *d_g,
                                    double const *d_x, double *d_out, void *stream);

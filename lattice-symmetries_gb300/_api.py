@@ -405,6 +405,14 @@ class SpinfulFermionBasis(Basis):
         return (1 << p) - 1, ((1 << p) - 1) << (2 * n - p)
 
 
+def split_terms(basis: Basis, expression: Expr):
+    """(off-diagonal, diagonal) non-branching terms of `expression` on `basis` (Operator.hs:109-135)."""
+    n_sites = getattr(basis, "number_sites", None) or getattr(basis, "number_spins")
+    spinful = isinstance(basis, SpinfulFermionBasis)
+    terms = expression.nonbranching_terms(n_sites, spinful=spinful)
+    return [t for t in terms if t[4] != 0], [t for t in terms if t[4] == 0]
+
+
 def _terms_struct(arrays, number_bits: int, keep: list):
     v, m, l, r, x, s = arrays
     n = len(v)
@@ -431,15 +439,22 @@ class Operator(_LinearOperator):
             raise TypeError("expected a 'Basis', but got '{}'".format(type(basis)))
         if not isinstance(expression, Expr):
             raise TypeError("expected an 'Expr', but got '{}'".format(type(expression)))
+        off, diag = split_terms(basis, expression)
+        self._setup(basis, expression, terms_to_arrays(off), terms_to_arrays(diag))
+
+    @classmethod
+    def _from_arrays(cls, basis: Basis, off_arrays, diag_arrays, expression: Optional[Expr] = None):
+        """An operator from raw non-branching term arrays (v, m, l, r, x, s); the arrays are kept
+        and read by the library on every call, so changing v in place re-parametrises it."""
+        op = cls.__new__(cls)
+        op._setup(basis, expression, off_arrays, diag_arrays)
+        return op
+
+    def _setup(self, basis, expression, off_arrays, diag_arrays):
         self._basis = basis
         self._expression = expression
-        n_sites = getattr(basis, "number_sites", None) or getattr(basis, "number_spins")
-        spinful = isinstance(basis, SpinfulFermionBasis)
-        terms = expression.nonbranching_terms(n_sites, spinful=spinful)
-        diag = [t for t in terms if t[4] == 0]
-        off = [t for t in terms if t[4] != 0]
-        self._diag_arrays = terms_to_arrays(diag)
-        self._off_arrays = terms_to_arrays(off)
+        self._off_arrays = tuple(np.ascontiguousarray(a) for a in off_arrays)
+        self._diag_arrays = tuple(np.ascontiguousarray(a) for a in diag_arrays)
         self._keep = []
         nb = basis.number_bits
         self._c_off = _terms_struct(self._off_arrays, nb, self._keep)

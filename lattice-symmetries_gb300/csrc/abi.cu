@@ -1302,8 +1302,32 @@ extern "C" int ls_gpu_state_index(ls_hs_basis const* basis, int64_t batch, uint6
 extern "C" int ls_gpu_coupling_inner_products(ls_hs_operator const* op, int n_couplings,
                                               int32_t const* term_coupling, double const* d_g,
                                               double const* d_x, double* d_out, void* stream) {
-  (void)op; (void)n_couplings; (void)term_coupling; (void)d_g; (void)d_x; (void)d_out; (void)stream;
-  return fail(LS_GPU_ERR_INVALID, "not implemented yet");
+  if (op == nullptr || term_coupling == nullptr || d_g == nullptr || d_x == nullptr || d_out == nullptr)
+    return fail(LS_GPU_ERR_INVALID, "NULL argument");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  MatvecProblem p;
+  int rc = make_problem(op, false, &p);
+  if (rc != 0) return rc;
+  OperatorCache* c = g_ops[op];
+  const int n_terms = c->off.n + c->diag.n;
+  for (int t = 0; t < n_terms; ++t)
+    if (term_coupling[t] < 0 || term_coupling[t] >= n_couplings)
+      return fail(LS_GPU_ERR_INVALID, "term coupling id out of range");
+  if (c->d_coupling == nullptr || c->coupling.size() != (size_t)n_terms ||
+      memcmp(c->coupling.data(), term_coupling, (size_t)n_terms * 4) != 0) {
+    if (c->d_coupling) cudaFree(c->d_coupling);
+    c->d_coupling = nullptr;
+    c->coupling.assign(term_coupling, term_coupling + n_terms);
+    if (!cuda_ok(cudaMalloc((void**)&c->d_coupling, (size_t)std::max(n_terms, 1) * 4), "cudaMalloc(couplings)") ||
+        !cuda_ok(cudaMemcpy(c->d_coupling, c->coupling.data(), (size_t)n_terms * 4, cudaMemcpyHostToDevice),
+                 "upload couplings")) {
+      c->coupling.clear();
+      return LS_GPU_ERR_CUDA;
+    }
+  }
+  p.off.coupling = c->d_coupling;
+  p.diag.coupling = c->d_coupling + c->off.n;
+  return launch_coupling_products(p, n_couplings, d_g, d_x, d_out, device_error_word(), (cudaStream_t)stream);
 }
 
 namespace {
