@@ -302,6 +302,16 @@ int ls_gpu_coupling_inner_products(ls_hs_operator const *op, int n_couplings,
                                    int32_t const *term_coupling, double const *d_g,
                                    double const *d_x, double *d_out, void *stream);
 
+/* Orbit-scan data for spinful fermions with lattice symmetries: `group` permutes the 2n orbitals
+ * (up site k -> orbital k, down site k -> orbital n + k; the same site permutation on both
+ * species) and carries the characters.  Every element acts on Fock states with the sign of the
+ * permutation it induces on the occupied orbitals, in state_info, is_representative, the norms,
+ * the enumeration (which needs fixed N_up, N_down and keeps a state iff its stabiliser acts
+ * trivially) and the matvec.  Install it in ls_hs_basis_kernels like the spin kernel data and set
+ * requires_projection.  No counterpart in the reference, whose fermionic bases have no lattice
+ * symmetries (Basis.hs:713-723).  Destroy with ls_internal_destroy_halide_kernel_data. */
+void *ls_gpu_create_fermionic_kernel_data(ls_hs_permutation_group const *group, int number_sites);
+
 /* Membership rule of the projected enumeration behind ls_hs_build_representatives and
  * ls_chpl_enumerate_representatives: 0 (default) keeps a state iff the reference's floating
  * stabiliser sum is positive (StatesEnumeration.chpl:242-268), 1 iff its stabiliser has only

@@ -66,7 +66,7 @@ class Basis:
         c.number_up = number_up
         c.particle_type = particle_type
         c.spin_inversion = spin_inversion
-        has_perm = particle_type == N.LS_HS_SPIN and self._symmetries.order > 0
+        has_perm = particle_type in (N.LS_HS_SPIN, N.LS_HS_SPINFUL_FERMION) and self._symmetries.order > 0
         c.requires_projection = bool(has_perm or spin_inversion != 0)
         c.state_index_is_identity = self._index_is_identity()
         c.kernels = ctypes.pointer(self._c_kernels)
@@ -100,7 +100,10 @@ class Basis:
         g.shifts = N.as_ptr(shifts, c_uint64)
         g.eigvals_re = N.as_ptr(re, c_double)
         g.eigvals_im = N.as_ptr(im, c_double)
-        ptr = self._lib.ls_internal_create_halide_kernel_data(byref(g), int(self._c.spin_inversion))
+        if self._c.particle_type == N.LS_HS_SPINFUL_FERMION:
+            ptr = self._lib.ls_gpu_create_fermionic_kernel_data(byref(g), int(self._c.number_sites))
+        else:
+            ptr = self._lib.ls_internal_create_halide_kernel_data(byref(g), int(self._c.spin_inversion))
         N.check()
         if not ptr:
             raise RuntimeError("could not create the orbit-scan data")
@@ -362,9 +365,14 @@ class SpinlessFermionBasis(Basis):
 
 
 class SpinfulFermionBasis(Basis):
-    """Spinful fermions: bits [0, n) are the up spins, [n, 2n) the down spins (Basis.hs:621-628)."""
+    """Spinful fermions: bits [0, n) are the up spins, [n, 2n) the down spins (Basis.hs:621-628).
 
-    def __init__(self, number_sites: int, number_particles: Union[None, int, Tuple[int, int]] = None):
+    ``symmetries`` (an addition: the reference has no fermionic lattice symmetries,
+    Basis.hs:713-723) are site permutations; each acts on both spin species and on Fock states
+    with the sign of the permutation of the occupied orbitals.  They need fixed (N_up, N_down)."""
+
+    def __init__(self, number_sites: int, number_particles: Union[None, int, Tuple[int, int]] = None,
+                 symmetries: Optional[Symmetries] = None):
         n = int(number_sites)
         if n <= 0:
             raise ValueError("invalid number of sites: {}".format(n))
@@ -384,10 +392,18 @@ class SpinfulFermionBasis(Basis):
                 raise ValueError("invalid number of particles: {}".format(p))
             total, up = p, -1
             self.occupation = p
-        super().__init__(N.LS_HS_SPINFUL_FERMION, n, total, up, 0, None)
+        doubled = None
+        if symmetries is not None and symmetries.order > 0:
+            if symmetries.number_bits != n:
+                raise ValueError("symmetries act on {} sites, the basis has {}".format(symmetries.number_bits, n))
+            if not isinstance(self.occupation, tuple):
+                raise ValueError("lattice symmetries of spinful fermions need fixed (N_up, N_down)")
+            doubled = symmetries.doubled()
+        self.site_symmetries = symmetries
+        super().__init__(N.LS_HS_SPINFUL_FERMION, n, total, up, 0, doubled)
 
     def _index_is_identity(self) -> bool:
-        return self.occupation is None
+        return self.occupation is None and (self.site_symmetries is None or self.site_symmetries.order == 0)
 
     def _number_bits(self) -> int:
         return 2 * self.number_sites

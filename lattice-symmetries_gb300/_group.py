@@ -316,6 +316,15 @@ class Symmetries:
         """Group.hs:155-156: all imaginary parts of the characters are exactly zero."""
         return bool(np.all(self.characters[1] == 0))
 
+    def doubled(self) -> "Symmetries":
+        """The same group acting on spinful-fermion orbitals: site permutation p becomes
+        p on the up orbitals [0, n) and p + n on the down orbitals [n, 2n); elements keep their
+        order and characters."""
+        n = self.number_bits
+        gens = [Symmetry(list(g.permutation) + [n + int(i) for i in g.permutation], g.sector)
+                for g in self._generators]
+        return Symmetries(gens)
+
     def network(self) -> Tuple[np.ndarray, np.ndarray]:
         """Batched Benes network: masks [depth][|G|] (uint64) and shifts [depth] (uint64)."""
         if self._network is None:

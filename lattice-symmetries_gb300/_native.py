@@ -123,6 +123,7 @@ _SIGNATURES = [
     ("ls_chpl_finalize", None, []),
     ("ls_internal_create_halide_kernel_data", c_void_p, [POINTER(ls_hs_permutation_group), c_int]),
     ("ls_internal_destroy_halide_kernel_data", None, [c_void_p]),
+    ("ls_gpu_create_fermionic_kernel_data", c_void_p, [POINTER(ls_hs_permutation_group), c_int]),
     ("ls_hs_state_info", None, [POINTER(ls_hs_basis), c_ssize_t, POINTER(c_uint64), c_ssize_t,
                                 POINTER(c_uint64), c_ssize_t, POINTER(c_double), POINTER(c_double)]),
     ("ls_hs_is_representative", None, [POINTER(ls_hs_basis), c_ssize_t, POINTER(c_uint64), c_ssize_t,

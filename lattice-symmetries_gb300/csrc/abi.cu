@@ -246,8 +246,28 @@ extern "C" int ls_gpu_set_matvec_config(int threads_per_block, int blocks_per_sm
 // =================================================================================================
 // Orbit-scan kernel data (kernels.c:112-193)
 // =================================================================================================
+static void* create_orbit_data(ls_hs_permutation_group const* g, int spin_inversion, int fermionic_sites);
+
 extern "C" void* ls_internal_create_halide_kernel_data(ls_hs_permutation_group const* g,
                                                        int spin_inversion) {
+  return create_orbit_data(g, spin_inversion, 0);
+}
+
+// Orbit data of a lattice-symmetry group acting on spinful fermions: `g` permutes the 2n orbitals
+// (up k -> k, down k -> n + k) and carries the characters; every element acts with the sign of
+// the permutation it induces on the occupied orbitals.  No counterpart in the reference, whose
+// fermionic bases have no lattice symmetries (Basis.hs:713-723).
+extern "C" void* ls_gpu_create_fermionic_kernel_data(ls_hs_permutation_group const* g, int number_sites) {
+  if (g == nullptr || number_sites <= 0 || g->number_bits != 2 * number_sites) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    set_error("a fermionic group acts on 2 * number_sites orbitals");
+    report("ls_gpu_create_fermionic_kernel_data");
+    return nullptr;
+  }
+  return create_orbit_data(g, 0, number_sites);
+}
+
+static void* create_orbit_data(ls_hs_permutation_group const* g, int spin_inversion, int fermionic_sites) {
   std::lock_guard<std::mutex> lock(g_mutex);
   if (g == nullptr) {
     set_error("permutation group is NULL");
@@ -274,6 +294,7 @@ extern "C" void* ls_internal_create_halide_kernel_data(ls_hs_permutation_group c
   for (int k = 0; k < od->depth; ++k) od->shifts[k] = (uint32_t)g->shifts[k];
   od->chars_re.assign(g->eigvals_re, g->eigvals_re + od->n_elems);
   od->chars_im.assign(g->eigvals_im, g->eigvals_im + od->n_elems);
+  od->fermionic = fermionic_sites > 0 ? 1 : 0;
   if (compute_site_images(od) != 0) {
     report("ls_internal_create_halide_kernel_data");
     delete od;
@@ -545,7 +566,8 @@ static IndexData* basis_index(ls_hs_basis const* b) {
 
 static bool has_permutations(ls_hs_basis const* b) {
   const OrbitData* od = basis_orbit(b);
-  return b->particle_type == LS_HS_SPIN && od != nullptr && od->n_elems > 0;
+  if (od == nullptr || od->n_elems == 0) return false;
+  return b->particle_type == LS_HS_SPIN || (b->particle_type == LS_HS_SPINFUL_FERMION && od->fermionic);
 }
 
 static bool hamming_fixed(ls_hs_basis const* b) {
@@ -648,6 +670,12 @@ static int enumerate_into(ls_hs_basis const* b, uint64_t** d_out, int64_t* count
     } else {
       req.mode = 1;
     }
+  } else if (b->particle_type == LS_HS_SPINFUL_FERMION && has_permutations(b)) {
+    if (b->number_up < 0) return fail(LS_GPU_ERR_INVALID, "fermionic bases with lattice symmetries need fixed (N_up, N_down)");
+    req.mode = 3;
+    req.spin_inversion = 0;
+    g = orbit_device(od);
+    if (g == nullptr) return LS_GPU_ERR_CUDA;
   } else if (b->particle_type == LS_HS_SPINFUL_FERMION) {
     req.mode = b->number_up >= 0 ? 2 : 1;
     req.spin_inversion = 0;
@@ -685,6 +713,11 @@ extern "C" int ls_gpu_enumerate_noalloc(ls_hs_basis const* b, uint64_t* d_out, i
     } else {
       req.mode = 1;
     }
+  } else if (b->particle_type == LS_HS_SPINFUL_FERMION && has_permutations(b)) {
+    if (b->number_up < 0) return fail(LS_GPU_ERR_INVALID, "fermionic bases with lattice symmetries need fixed (N_up, N_down)");
+    req.mode = 3;
+    req.spin_inversion = 0;
+    od = basis_orbit(b);
   } else if (b->particle_type == LS_HS_SPINFUL_FERMION) {
     req.mode = b->number_up >= 0 ? 2 : 1;
     req.spin_inversion = 0;

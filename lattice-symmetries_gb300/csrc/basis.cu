@@ -187,7 +187,8 @@ __global__ void k_state_info(DeviceGroup g, int64_t n, const uint64_t* __restric
       }
       if (y == a) {
         ++count;
-        if (cre != 1.0) trivial = false;
+        const double sg = (g.fermionic && fermion_parity(g.fsign + (int64_t)e * g.n_bits, 1, a)) ? -1.0 : 1.0;
+        if (sg * cre != 1.0) trivial = false;
       }
       if (g.spin_inversion != 0) {
         const uint64_t yf = y ^ g.flip;
@@ -204,6 +205,7 @@ __global__ void k_state_info(DeviceGroup g, int64_t n, const uint64_t* __restric
     if (bestg >= 0) {
       ch = g.chars[bestg];
       if (bestf && g.spin_inversion == -1) ch = make_double2(-ch.x, -ch.y);
+      if (g.fermionic && fermion_parity(g.fsign + (int64_t)bestg * g.n_bits, 1, a)) ch = make_double2(-ch.x, -ch.y);
     }
     reps[i] = best;
     chars[i] = ch;
@@ -227,7 +229,8 @@ __global__ void k_orbit_norms(DeviceGroup g, int64_t n, const uint64_t* __restri
       const double cre = __ldg(&g.chars[e].x);
       if (y == a) {
         ++count;
-        if (cre != 1.0) trivial = false;
+        const double sg = (g.fermionic && fermion_parity(g.fsign + (int64_t)e * g.n_bits, 1, a)) ? -1.0 : 1.0;
+        if (sg * cre != 1.0) trivial = false;
       }
       if (g.spin_inversion != 0 && (y ^ g.flip) == a) {
         ++count;
@@ -256,11 +259,13 @@ __device__ __forceinline__ void ir_term(const DeviceGroup& g, uint64_t a, int e,
   const double cre = __ldg(&g.chars[e].x);
   if (g.spin_inversion == 0) {
     const bool eq = (y == a);
-    s = eq ? cre : 0.0;
+    double c = cre;
+    if (eq && g.fermionic && fermion_parity(g.fsign + (int64_t)e * g.n_bits, 1, a)) c = -cre;
+    s = eq ? c : 0.0;
     ge = y >= a;
     if (eq) {
       ++cnt;
-      if (cre != 1.0) trivial = false;
+      if (c != 1.0) trivial = false;
     }
   } else {
     const uint64_t yf = y ^ g.flip;
@@ -469,8 +474,29 @@ int compute_site_images(OrbitData* od) {
   }
   od->gpl = gpl > 0 ? gpl : 0;
 
+  // Fermionic sign tables: g moves orbital k to g(k) = position of the image of 1 << k, and
+  // L_g[k] holds the orbitals l < k with g(l) > g(k) (the pairs whose order g reverses).
+  std::vector<uint64_t> fsign, fsign_packed;
+  if (od->fermionic) {
+    fsign.assign((size_t)G * B, 0);
+    for (int e = 0; e < G; ++e) {
+      for (int k = 0; k < B; ++k) {
+        const int gk = __builtin_ctzll(onehot[(size_t)k * G + e]);
+        uint64_t m = 0;
+        for (int l = 0; l < k; ++l)
+          if (__builtin_ctzll(onehot[(size_t)l * G + e]) > gk) m |= (uint64_t)1 << l;
+        fsign[(size_t)e * B + k] = m;
+      }
+    }
+    fsign_packed.assign((size_t)B * Gp, 0);
+    for (int s = 0; s < Gp; ++s) {
+      const int e = s < G ? s : 0;
+      for (int k = 0; k < B; ++k) fsign_packed[(size_t)k * Gp + s] = fsign[(size_t)e * B + k];
+    }
+  }
+
   // One block: masks_t | shifts | chars | onehot | prio | onehot_packed | chars_packed
-  // (16-byte aligned pieces).
+  // [| fsign | fsign_packed] (16-byte aligned pieces).
   auto align16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
   od->off_masks = 0;
   od->off_shifts = align16(od->off_masks + masks_t.size() * 8);
@@ -479,7 +505,9 @@ int compute_site_images(OrbitData* od) {
   od->off_prio = align16(od->off_onehot + std::max<size_t>(onehot.size(), 1) * 8);
   od->off_onehot_packed = align16(od->off_prio + (size_t)std::max(G, 1) * 2);
   od->off_chars_packed = align16(od->off_onehot_packed + std::max<size_t>(onehot_packed.size(), 1) * 8);
-  const size_t total = align16(od->off_chars_packed + (size_t)std::max(Gp, 1) * 16) + 16;
+  od->off_fsign = align16(od->off_chars_packed + (size_t)std::max(Gp, 1) * 16);
+  od->off_fsign_packed = align16(od->off_fsign + fsign.size() * 8);
+  const size_t total = align16(od->off_fsign_packed + fsign_packed.size() * 8) + 16;
   od->host_block.assign(total, 0);
   uint8_t* h = od->host_block.data();
   if (!masks_t.empty()) memcpy(h + od->off_masks, masks_t.data(), masks_t.size() * 8);
@@ -490,6 +518,8 @@ int compute_site_images(OrbitData* od) {
   if (!onehot_packed.empty())
     memcpy(h + od->off_onehot_packed, onehot_packed.data(), onehot_packed.size() * 8);
   if (Gp > 0) memcpy(h + od->off_chars_packed, chars_packed.data(), (size_t)Gp * 16);
+  if (!fsign.empty()) memcpy(h + od->off_fsign, fsign.data(), fsign.size() * 8);
+  if (!fsign_packed.empty()) memcpy(h + od->off_fsign_packed, fsign_packed.data(), fsign_packed.size() * 8);
   DeviceGroup probe;
   od->standard_shifts = standard_shifts(probe, od->shifts);
   return 0;
@@ -526,6 +556,9 @@ const DeviceGroup* orbit_device(const OrbitData* od) {
   g.gpl = od->gpl;
   g.onehot_packed = od->gpl > 0 ? (const uint64_t*)(base + od->off_onehot_packed) : nullptr;
   g.chars_packed = od->gpl > 0 ? (const double2*)(base + od->off_chars_packed) : nullptr;
+  g.fermionic = od->fermionic;
+  g.fsign = od->fermionic ? (const uint64_t*)(base + od->off_fsign) : nullptr;
+  g.fsign_packed = (od->fermionic && od->gpl > 0) ? (const uint64_t*)(base + od->off_fsign_packed) : nullptr;
   od->dev_block = d;
   od->dev_device = dev;
   return &od->dev;
@@ -648,13 +681,67 @@ struct EnumArgs {
   uint64_t* append;
   int64_t capacity;
   unsigned long long* counter;
+  // Spinful fermions (mode 3): candidate (iB, iA) = (idx / nA, idx % nA) is
+  // unrank(rankB + iB, hB) << ns | unrank(rankA + iA, hA), ascending.
+  int spinful;
+  int ns, hA, hB;
+  int64_t rankA, rankB, nA;
+  uint64_t minA, maxA;
 };
 
 __device__ inline uint64_t candidate_at(const EnumArgs& a, int64_t idx) {
+  if (a.spinful) {
+    const int64_t iB = idx / a.nA, iA = idx - iB * a.nA;
+    return (d_unrank(a.rankB + iB, a.hB, a.ns) << a.ns) | d_unrank(a.rankA + iA, a.hA, a.ns);
+  }
   return a.h >= 0 ? d_unrank(a.first_rank + idx, a.h, a.n_bits) : (uint64_t)(a.first_rank + idx);
 }
+// Successor of candidate v (only called while another candidate follows in the range).
 __device__ inline uint64_t candidate_next(const EnumArgs& a, uint64_t v) {
+  if (a.spinful) {
+    const uint64_t mask = (~0ull) >> (64 - a.ns);
+    const uint64_t A = v & mask;
+    if (A == a.maxA) return (next_fixed_hamming(v >> a.ns) << a.ns) | a.minA;
+    return (v & ~mask) | next_fixed_hamming(A);
+  }
   return a.h >= 0 ? next_fixed_hamming(v) : v + 1;
+}
+
+// Candidate range of a projected enumeration: fixed Hamming weight / all states of n_bits
+// (mode 0), or the (N_up, N_down) product range of spinful fermions (mode 3).
+static void projected_candidates(const EnumerateRequest& req, int n_bits, EnumArgs* a) {
+  a->n_bits = n_bits;
+  a->lane_width = 4;
+  a->reference_rule = req.reference_norm_rule;
+  if (req.mode == 3) {
+    const int ns = req.number_sites;
+    const uint64_t mask = (~0ull) >> (64 - ns);
+    a->spinful = 1;
+    a->h = -1;
+    a->ns = ns;
+    a->minA = req.lower & mask;
+    a->maxA = req.upper & mask;
+    const uint64_t minB = (req.lower >> ns) & mask, maxB = (req.upper >> ns) & mask;
+    a->hA = __builtin_popcountll(a->minA);
+    a->hB = __builtin_popcountll(minB);
+    a->rankA = fixed_hamming_state_to_index(a->minA);
+    a->nA = fixed_hamming_state_to_index(a->maxA) - a->rankA + 1;
+    a->rankB = fixed_hamming_state_to_index(minB);
+    const int64_t nB = fixed_hamming_state_to_index(maxB) - a->rankB + 1;
+    a->n_candidates = a->nA * nB;
+    a->reference_rule = 0;  // no floating rule for fermionic signs: exact stabiliser rule
+  } else {
+    a->spinful = 0;
+    a->h = req.hamming_fixed ? __builtin_popcountll(req.lower) : -1;
+    if (a->h >= 0) {
+      a->first_rank = fixed_hamming_state_to_index(req.lower);
+      a->n_candidates = fixed_hamming_state_to_index(req.upper) - a->first_rank + 1;
+    } else {
+      a->first_rank = (int64_t)req.lower;
+      a->n_candidates = (int64_t)(req.upper - req.lower) + 1;
+    }
+  }
+  a->n_tiles = (a->n_candidates + kEnumTile - 1) / kEnumTile;
 }
 
 template <int DEPTH>
@@ -770,7 +857,7 @@ int enumerate_states(const DeviceGroup* g0, const EnumerateRequest& req, uint64_
   *d_out = nullptr;
   *count = 0;
   if (ensure_binomials() != 0) return LS_GPU_ERR_CUDA;
-  const int n_bits = req.mode == 2 ? 2 * req.number_sites : req.number_sites;
+  const int n_bits = (req.mode == 2 || req.mode == 3) ? 2 * req.number_sites : req.number_sites;
   if (req.lower > req.upper) return 0;
   if (req.mode == 1) {
     uint64_t low = req.lower, high = req.upper;
@@ -829,18 +916,7 @@ int enumerate_states(const DeviceGroup* g0, const EnumerateRequest& req, uint64_
   if (g0 == nullptr || g0->n_elems == 0) return fail(LS_GPU_ERR_INVALID, "projected enumeration without a group");
   DeviceGroup g = strip(*g0);
   EnumArgs a{};
-  a.h = req.hamming_fixed ? __builtin_popcountll(req.lower) : -1;
-  a.n_bits = n_bits;
-  a.lane_width = 4;
-  a.reference_rule = req.reference_norm_rule;
-  if (a.h >= 0) {
-    a.first_rank = fixed_hamming_state_to_index(req.lower);
-    a.n_candidates = fixed_hamming_state_to_index(req.upper) - a.first_rank + 1;
-  } else {
-    a.first_rank = (int64_t)req.lower;
-    a.n_candidates = (int64_t)(req.upper - req.lower) + 1;
-  }
-  a.n_tiles = (a.n_candidates + kEnumTile - 1) / kEnumTile;
+  projected_candidates(req, n_bits, &a);
   // Capacity guess: candidates / |G| * 2 + slack; retried with the exact count on overflow.
   int64_t capacity = std::min<int64_t>(a.n_candidates,
                                        a.n_candidates / std::max(1, g.n_elems) * 2 + 1024 * 1024);
@@ -1146,7 +1222,7 @@ int enumerate_states_noalloc(const OrbitData* od, const EnumerateRequest& req, u
   *count = 0;
   if (capacity < 0) return fail(LS_GPU_ERR_INVALID, "negative capacity");
   if (ensure_binomials() != 0) return LS_GPU_ERR_CUDA;
-  const int n_bits = req.mode == 2 ? 2 * req.number_sites : req.number_sites;
+  const int n_bits = (req.mode == 2 || req.mode == 3) ? 2 * req.number_sites : req.number_sites;
   if (req.lower > req.upper) return 0;
   if (req.mode == 1 || req.mode == 2) {
     // No scratch needed: the states are generated directly from their combinadic ranks.
@@ -1199,18 +1275,7 @@ int enumerate_states_noalloc(const OrbitData* od, const EnumerateRequest& req, u
   if (group_bytes > kNoallocGroupBytes)
     return fail(LS_GPU_ERR_INVALID, "symmetry group tables exceed the 1 MiB reserved for them");
   EnumArgs a{};
-  a.h = req.hamming_fixed ? __builtin_popcountll(req.lower) : -1;
-  a.n_bits = n_bits;
-  a.lane_width = 4;
-  a.reference_rule = req.reference_norm_rule;
-  if (a.h >= 0) {
-    a.first_rank = fixed_hamming_state_to_index(req.lower);
-    a.n_candidates = fixed_hamming_state_to_index(req.upper) - a.first_rank + 1;
-  } else {
-    a.first_rank = (int64_t)req.lower;
-    a.n_candidates = (int64_t)(req.upper - req.lower) + 1;
-  }
-  a.n_tiles = (a.n_candidates + kEnumTile - 1) / kEnumTile;
+  projected_candidates(req, n_bits, &a);
   // tile counts | tile offsets (n + 1) | block sums | scanned block sums (+ total)
   const int64_t max_tiles =
       (int64_t)((kNoallocScratchBytes - kNoallocGroupBytes - 4 * 65536) / (4 + 8)) - 1;
@@ -1243,6 +1308,8 @@ int enumerate_states_noalloc(const OrbitData* od, const EnumerateRequest& req, u
   g.chars = (const double2*)(base + od->off_chars);
   g.onehot = (const uint64_t*)(base + od->off_onehot);
   g.prio = (const uint16_t*)(base + od->off_prio);
+  g.fermionic = od->fermionic;
+  g.fsign = od->fermionic ? (const uint64_t*)(base + od->off_fsign) : nullptr;
 
   dispatch_depth<RunEnumerateNoalloc>(g.depth, od->standard_shifts, g, a, counts, offsets, d_out, capacity, 0, s);
   if (!cuda_ok(cudaGetLastError(), "k_enumerate_count")) return LS_GPU_ERR_CUDA;

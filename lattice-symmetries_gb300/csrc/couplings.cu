@@ -195,6 +195,7 @@ int launch_coupling_products(const MatvecProblem& p, int nc, const double* d_g, 
   if (p.projection != 2 || p.group.gpl < 1 || p.group.gpl > 4 || p.group.onehot_packed == nullptr)
     return fail(LS_GPU_ERR_INVALID, "the fused coupling kernel needs a basis with lattice symmetries of at most "
                                     "128 elements");
+  if (p.group.fermionic) return fail(LS_GPU_ERR_INVALID, "the fused coupling kernel has no fermionic signs");
   if (p.off.coupling == nullptr) return fail(LS_GPU_ERR_INVALID, "operator terms carry no coupling ids");
   const uint64_t* binom = device_binomials();
   if (binom == nullptr) return LS_GPU_ERR_CUDA;

@@ -34,7 +34,30 @@ struct DeviceGroup {
   int gpl = 0;                              // slots per lane (0: packed tables unavailable)
   const uint64_t* onehot_packed = nullptr;  // [n_bits][gpl * 32]
   const double2* chars_packed = nullptr;    // [gpl * 32]
+  // Fermionic groups (spinful fermions with lattice symmetries): g acts on Fock states with the
+  // sign of the permutation it induces on the occupied orbitals.  inv_g(x) = sum over occupied k
+  // of popcount(x & L_g[k]), L_g[k] = orbitals l < k that g moves past k; the sign is
+  // (-1)^inv_g(x).
+  int fermionic = 0;
+  const uint64_t* fsign = nullptr;          // [n_elems][n_bits]: L_g[k]
+  const uint64_t* fsign_packed = nullptr;   // [n_bits][gpl * 32], slot-padded like onehot_packed
 };
+
+// (-1)^inv parity of a fermionic group element on `state`: L points to L_g[0] and consecutive
+// orbitals are `stride` words apart.
+__host__ __device__ inline int fermion_parity(const uint64_t* L, int stride, uint64_t state) {
+  int inv = 0;
+  for (uint64_t bits = state; bits != 0; bits &= bits - 1) {
+#ifdef __CUDA_ARCH__
+    const int k = __ffsll((long long)bits) - 1;
+    inv += __popcll(state & L[(size_t)k * stride]);
+#else
+    const int k = __builtin_ctzll(bits);
+    inv += __builtin_popcountll(state & L[(size_t)k * stride]);
+#endif
+  }
+  return inv & 1;
+}
 
 // Slots per lane of the matvec kernels for a group of n elements (ascending choices).
 constexpr int kGplSet[] = {1, 2, 3, 4, 6, 9, 12, 16};
@@ -97,7 +120,9 @@ struct OrbitData {
   std::vector<uint8_t> host_block;
   size_t off_masks = 0, off_shifts = 0, off_chars = 0, off_onehot = 0, off_prio = 0;
   size_t off_onehot_packed = 0, off_chars_packed = 0;
+  size_t off_fsign = 0, off_fsign_packed = 0;  // fermionic groups only
   int gpl = 0;  // packed tables present when > 0
+  int fermionic = 0;
   bool standard_shifts = true;
   mutable DeviceGroup dev;
   mutable void* dev_block = nullptr;  // one allocation holding all device arrays
@@ -141,7 +166,8 @@ int compute_site_images(OrbitData* od);          // host tables (no GPU needed)
 const DeviceGroup* orbit_device(const OrbitData* od);  // uploads on first use; null on failure
 
 struct EnumerateRequest {
-  int mode;              // 0 projected spin, 1 unprojected (fixed weight or all), 2 spinful per sector
+  int mode;              // 0 projected spin, 1 unprojected (fixed weight or all), 2 spinful per
+                         // sector, 3 projected spinful fermions (fixed N_up, N_down)
   int hamming_fixed;
   int number_sites;
   int spin_inversion;

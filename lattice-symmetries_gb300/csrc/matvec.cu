@@ -9,6 +9,10 @@ namespace lsg {
 int launch_packed(bool cplx, int k, int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L,
                   LaunchShape sh, const double* x, int64_t ldx, double* y, int64_t ldy, int* err,
                   const uint64_t* binom, cudaStream_t s) {
+  if (p.group.fermionic) {
+    if (inv) return fail(LS_GPU_ERR_INVALID, "fermionic groups have no spin inversion");
+    return launch_packed_fermi(cplx, k, gpl, p, L, sh, x, ldx, y, ldy, err, binom, s);
+  }
   if (!cplx) {
     if (k != 1) return LS_GPU_ERR_INVALID;
     return launch_packed_real(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
@@ -73,6 +77,8 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
       }
       return 0;
     }
+    if (p.group.fermionic)
+      return fail(LS_GPU_ERR_INVALID, "fermionic lattice symmetries need the packed kernel (tables too large)");
     const int gpl = pick_gpl_for(p.group.n_elems);
     if (gpl < 0) return fail(LS_GPU_ERR_INVALID, "symmetry group too large for the matvec kernels");
     const SmemLayout L = make_layout(p, true);
@@ -131,7 +137,7 @@ int sector_plan_build(const std::vector<MatvecProblem>& problems, bool shareable
   plan->xs = xs;
   plan->ys = ys;
   const MatvecProblem& p0 = problems[0];
-  plan->batched = shareable && n <= kMaxSectors && p0.projection == 2 && p0.group.gpl >= 1 &&
+  plan->batched = shareable && n <= kMaxSectors && p0.projection == 2 && !p0.group.fermionic && p0.group.gpl >= 1 &&
                   p0.group.gpl <= kSectorMaxGpl && p0.group.onehot_packed != nullptr;
   if (plan->batched) {
     plan->shared = p0;

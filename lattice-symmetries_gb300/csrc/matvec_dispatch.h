@@ -33,6 +33,11 @@ LSG_DECLARE_PACKED(launch_packed_cplx_k4)
 LSG_DECLARE_PACKED(launch_packed_cplx_k8)
 LSG_DECLARE_PACKED(launch_packed_cplx_k16)
 
+// Packed kernel for fermionic groups (gpl <= 4): real (k = 1) or complex (k in {1, 4, 8, 16}).
+int launch_packed_fermi(bool cplx, int k, int gpl, const MatvecProblem& p, const PackedLayout& L, LaunchShape sh,
+                        const double* x, int64_t ldx, double* y, int64_t ldy, int* err, const uint64_t* binom,
+                        cudaStream_t s);
+
 // Batched multi-sector kernel (complex, k in {1, 4, 8, 16}, gpl in {1, 2, 3, 4}).
 struct SectorDesc;
 int launch_sectors(int k, int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L, LaunchShape sh,

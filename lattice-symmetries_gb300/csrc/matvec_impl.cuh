@@ -376,6 +376,7 @@ __global__ void __launch_bounds__(256, 2)
 struct PackedLayout {
   size_t off_onehot, off_chars, off_tm, off_tl, off_tx, off_ts, off_tv, off_ti, off_dm, off_dr, off_ds, off_dv;
   size_t off_sectors;  // sector table of the batched kernel (n_sectors > 0)
+  size_t off_fsign;    // fermionic sign tables [n_bits][gpl * 32] (fermionic groups)
   size_t total;
 };
 
@@ -410,6 +411,7 @@ inline PackedLayout make_packed_layout(const MatvecProblem& p, int n_sectors = 0
   L.off_ds = o; o = al(o + (size_t)p.diag.n * 8);
   L.off_dv = o; o = al(o + (size_t)p.diag.n * 16);
   L.off_sectors = o; o = al(o + (size_t)n_sectors * sizeof(SectorDesc));
+  L.off_fsign = o; o = al(o + (p.group.fermionic ? (size_t)p.group.n_bits * Gp * 8 : 0));
   L.total = o;
   return L;
 }
@@ -429,6 +431,7 @@ struct PackedTables {
   const uint32_t* ti;
   const uint64_t *dm, *dr, *ds;
   const double2* dv;
+  const uint64_t* fs;  // fermionic sign tables (fermionic groups)
   int nt, nd;
 };
 
@@ -462,6 +465,9 @@ __device__ __forceinline__ PackedTables stage_packed(const MatvecProblem& p, con
   stage_u64(dr, p.diag.r, p.diag.n);
   stage_u64(ds, p.diag.s, p.diag.n);
   stage_d2(dv, p.diag.v, p.diag.n);
+  uint64_t* fs = (uint64_t*)(smem + L.off_fsign);
+  if (p.group.fermionic) stage_u64(fs, p.group.fsign_packed, p.group.n_bits * Gp);
+  T.fs = fs;
   T.oh = oh; T.ch = ch; T.tm = tm; T.tl = tl; T.tx = tx; T.ts = ts; T.tv = tv; T.ti = ti;
   T.dm = dm; T.dr = dr; T.ds = ds; T.dv = dv;
   T.nt = p.off.n;
@@ -471,7 +477,7 @@ __device__ __forceinline__ PackedTables stage_packed(const MatvecProblem& p, con
 
 // One output row of the packed kernels (executed by a whole warp): y[row, 0..K) for the sector
 // described by (ix, chars, spin_inversion, x, y).
-template <int GPL, bool INV, bool CPLX, int K>
+template <int GPL, bool INV, bool CPLX, int K, bool FERMI = false>
 __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbits, const DeviceIndex& ix,
                                            const double2* __restrict__ chars, const int spin_inversion,
                                            const DeviceConstraint& cons, const double* __restrict__ x,
@@ -529,6 +535,7 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
   Acc acc;
   unsigned found = 0;
   uint64_t my_key = ~0ull;
+  uint64_t my_beta = 0;  // the generated state (fermionic groups: its sign under the winning element)
   double2 my_c = make_double2(0.0, 0.0);
   int nslot = 0;
 
@@ -545,6 +552,11 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
       if (j >= 0) {
         double2 chi = chars[idx >> 1];
         if (INV && (idx & 1) && spin_inversion == -1) chi = make_double2(-chi.x, -chi.y);
+        if constexpr (FERMI) {
+          // g moves the fermions of beta onto the representative with the sign of the
+          // permutation it induces on the occupied orbitals (one lane per element)
+          if (fermion_parity(T.fs + (idx >> 1), Gp, my_beta)) chi = make_double2(-chi.x, -chi.y);
+        }
         const C2 f = cmul_conj_b(C2{my_c.x, my_c.y}, C2{chi.x, chi.y});
         fre = f.re * nj;
         fim = f.im * nj;
@@ -623,6 +635,7 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
       if (lane == nslot) {
         my_key = ((uint64_t)mhi << 32) | mlo;
         my_c = c;
+        if constexpr (FERMI) my_beta = beta;
       }
       if (++nslot == 32) {
         flush();
@@ -657,7 +670,7 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
   }
 }
 
-template <int GPL, bool INV, bool CPLX, int K>
+template <int GPL, bool INV, bool CPLX, int K, bool FERMI = false>
 __global__ void __launch_bounds__(320, 2)
     k_matvec_packed(const MatvecProblem p, const PackedLayout L, const double* __restrict__ x, int64_t ldx,
                     double* __restrict__ y, int64_t ldy, int* __restrict__ err,
@@ -668,7 +681,7 @@ __global__ void __launch_bounds__(320, 2)
   const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t row = warp_id; row < p.n_rows; row += n_warps)
-    packed_row<GPL, INV, CPLX, K>(T, p.group.n_bits, p.index, T.ch, p.group.spin_inversion, p.constraint, x, ldx,
+    packed_row<GPL, INV, CPLX, K, FERMI>(T, p.group.n_bits, p.index, T.ch, p.group.spin_inversion, p.constraint, x, ldx,
                                   y, ldy, row, err, binom, p.nnz_counter);
 }
 
