@@ -25,26 +25,22 @@ from typing import Callable, List, Optional, Tuple
 import numpy as np
 
 
-def _row_chunks(D: int) -> int:
-    """Largest power of two c <= 256 with D % c == 0 and D / c >= 64: the row blocks of a Gram
-    product, so that the reduction over D runs as c independent GEMMs per sector."""
-    c = 1
-    while c < 256 and D % (2 * c) == 0 and D // (2 * c) >= 64:
-        c *= 2
-    return c
-
-
-def _gram(X, Y):
+def _gram(X, Y, blocks: int = 256, min_rows: int = 64):
     """X^H Y for [S, D, k] blocks as [S, k, k].  A single GEMM with inner dimension D (hundreds of
-    thousands) and a 16 x 16 output leaves most of the GPU idle; splitting D into row blocks gives
-    S * c GEMMs whose partial results are summed."""
+    thousands) and a 16 x 16 output leaves most of the GPU idle, so the rows are split into
+    `blocks` equal row blocks (S * blocks GEMMs whose partial results are summed) plus the
+    remaining D mod blocks rows."""
     S, D, k = X.shape
-    c = _row_chunks(D)
-    if c == 1:
+    c = blocks
+    while c > 1 and D // c < min_rows:
+        c //= 2
+    m = D // c
+    if c <= 1:
         return X.mH @ Y
-    Xc = X.reshape(S, c, D // c, k)
-    Yc = Y.reshape(S, c, D // c, k)
-    return (Xc.mH @ Yc).sum(1)
+    main = (X[:, :c * m].reshape(S, c, m, k).mH @ Y[:, :c * m].reshape(S, c, m, k)).sum(1)
+    if c * m == D:
+        return main
+    return main + X[:, c * m:].mH @ Y[:, c * m:]
 
 
 def _cholqr(W, eps: float = 1e-15):
@@ -186,3 +182,123 @@ def sector_ground_states(batch, steps: int, seed: int = 0, graph: bool = True,
     ev = block_lanczos(lambda: batch.run(), batch.X, batch.Y, steps, graph=graph, timer=timer)
     batch.check_errors()
     return ev[:, 0].cpu().numpy()
+
+
+def ground_state(apply: Callable[[], None], Q, W, steps: int, graph: bool = False,
+                 timer: Optional[dict] = None):
+    """Lowest eigenpair by block Lanczos with the Krylov blocks kept for the Ritz vector.
+
+    Q, W: [1, D, k] blocks (Q orthonormal on entry), `apply()` computes W = H Q.  Returns
+    (E0, psi0) with psi0 a unit vector [D] (complex128, on Q's device).  Memory: steps blocks of
+    [D, k]."""
+    import torch
+
+    S, D, k = Q.shape
+    if S != 1:
+        raise ValueError("ground_state handles one sector")
+    Qp = torch.zeros_like(Q)
+    Bp = torch.zeros((S, k, k), dtype=Q.dtype, device=Q.device)
+    A_cur = torch.zeros_like(Bp)
+    B_cur = torch.zeros_like(Bp)
+    A_hist, B_hist, blocks = [], [], []
+
+    def step_and_record(run):
+        blocks.append(Q[0].clone())
+        run()
+        A_hist.append(A_cur.clone())
+        B_hist.append(B_cur.clone())
+
+    def eager():
+        lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur)
+
+    g = None
+    if graph and Q.is_cuda:
+        side = torch.cuda.Stream(Q.device)
+        side.wait_stream(torch.cuda.current_stream(Q.device))
+        with torch.cuda.stream(side):
+            blocks.append(Q[0].clone())
+            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur)
+        torch.cuda.current_stream(Q.device).wait_stream(side)
+        A_hist.append(A_cur.clone())
+        B_hist.append(B_cur.clone())
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur)
+    start = end = None
+    if timer is not None and Q.is_cuda:
+        torch.cuda.synchronize(Q.device)
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record()
+    j0 = len(A_hist)
+    for _ in range(j0, steps):
+        step_and_record(g.replay if g is not None else eager)
+    if start is not None:
+        end.record()
+        torch.cuda.synchronize(Q.device)
+        timer["ms"] = start.elapsed_time(end)
+        timer["steps"] = steps - j0
+    T = block_tridiagonal(A_hist, B_hist)[0]
+    evals, evecs = torch.linalg.eigh(T)
+    y = evecs[:, 0].reshape(len(blocks), k)
+    psi = torch.zeros(D, dtype=Q.dtype, device=Q.device)
+    for j, blk in enumerate(blocks):
+        psi += blk @ y[j]
+    psi /= torch.linalg.vector_norm(psi)
+    return float(evals[0].real), psi
+
+
+def _energy_function():
+    import torch
+
+    class GroundStateEnergy(torch.autograd.Function):
+        """E0(theta) of a ParametrizedOperator; backward by Hellmann-Feynman:
+        dE0/dtheta_c = <psi0| H_c |psi0> (real for Hermitian H_c), from the fused coupling
+        products or one matvec per coupling."""
+
+        @staticmethod
+        def forward(ctx, theta, pop, k, steps, seed, graph):
+            import numpy as np
+            pop.set_theta(theta.detach().cpu().numpy())
+            op = pop.operator
+            D = op.basis.number_states
+            dev = torch.device("cuda", torch.cuda.current_device())
+            gen = torch.Generator(device="cpu").manual_seed(seed)
+            Q = (torch.randn((1, D, k), generator=gen, dtype=torch.float64)
+                 + 1j * torch.randn((1, D, k), generator=gen, dtype=torch.float64)).to(dev)
+            Q, _ = _cholqr(Q)
+            W = torch.empty_like(Q)
+            Q = Q.contiguous()
+
+            def apply():
+                op.apply_device(Q[0], out=W[0], check=False)
+
+            e0, psi = ground_state(apply, Q, W, steps, graph=graph)
+            op.check_errors()
+            ctx.pop = pop
+            ctx.psi = psi
+            ctx.save_for_backward(theta)
+            return torch.tensor(e0, dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, grad):
+            (theta,) = ctx.saved_tensors
+            hf = ctx.pop.coupling_products(ctx.psi, ctx.psi).real
+            return (grad.to(hf.device) * hf).to(dtype=theta.dtype, device=theta.device), None, None, None, None, None
+
+    return GroundStateEnergy
+
+
+_GSE = None
+
+
+def ground_state_energy(pop, theta, k: int = 8, steps: int = 60, seed: int = 0, graph: bool = True):
+    """E0(theta) of a ParametrizedOperator by k-RHS block Lanczos, differentiable in theta."""
+    import torch
+
+    global _GSE
+    if _GSE is None:
+        _GSE = _energy_function()
+    if not isinstance(theta, torch.Tensor):
+        theta = torch.as_tensor(theta, dtype=torch.float64)
+    return _GSE.apply(theta, pop, k, steps, seed, graph)

@@ -89,6 +89,14 @@ def ladder_symmetries(n_rungs: int, k: int = 0, exchange: int = 0) -> List[Symme
     return [Symmetry(t, k), Symmetry(ex, exchange)]
 
 
+def hubbard_parts(bonds, number_sites=None):
+    """(hopping with t = 1, on-site interaction with U = 1): H = t * hopping + U * interaction."""
+    hop = Expr("c†₀↑ c₁↑ + c†₁↑ c₀↑ + c†₀↓ c₁↓ + c†₁↓ c₀↓", sites=[list(b) for b in bonds]).scale(-1.0)
+    n = number_sites if number_sites is not None else 1 + max(max(b) for b in bonds)
+    onsite = Expr("n₀↑ n₀↓", sites=[[i] for i in range(n)])
+    return hop, onsite
+
+
 def hubbard(bonds, t=1.0, U=1.0, number_sites=None) -> Expr:
     hop = Expr("c†₀↑ c₁↑ + c†₁↑ c₀↑ + c†₀↓ c₁↓ + c†₁↓ c₀↓", sites=[list(b) for b in bonds]).scale(-t)
     n = number_sites if number_sites is not None else 1 + max(max(b) for b in bonds)

@@ -64,3 +64,17 @@ def test_block_lanczos_padded_sectors_are_independent():
     assert float(Q[1, 20:].abs().max()) == 0.0
     ref1 = np.linalg.eigvalsh(H[1, :20, :20].numpy())
     assert abs(float(ev[1, 0]) - ref1[0]) < 1e-9
+
+
+def test_ground_state_ritz_vector():
+    D, k = 50, 3
+    H = random_hermitian(1, D, seed=11)
+    g = torch.Generator().manual_seed(2)
+    Q = torch.randn((1, D, k), generator=g, dtype=torch.float64).to(torch.complex128)
+    Q, _ = lanczos._cholqr(Q)
+    W = torch.empty_like(Q)
+    e0, psi = lanczos.ground_state(lambda: W.copy_(H @ Q), Q, W, steps=20)
+    ref = torch.linalg.eigvalsh(H)[0, 0]
+    assert abs(e0 - float(ref)) < 1e-9
+    r = H[0] @ psi - e0 * psi
+    assert float(torch.linalg.vector_norm(r)) < 1e-6
