@@ -206,6 +206,7 @@ def run_reference(args):
     O.set_threads(threads)
     ls = importlib.import_module("lattice-symmetries_gb300")
     lat = importlib.import_module("lattice-symmetries_gb300.lattices")
+    rep = importlib.import_module("lattice-symmetries_gb300.replicas")
     basis, expr = build_workload(ls, lat, args.config)
     op = ls.Operator(basis, expr)
     gens = [(s.permutation, s.sector) for s in basis.symmetries.generators]
@@ -536,10 +537,11 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
-    if args.config == "xxz28_sectors":
-        return run_sectors(args)
-    if args.config == "hubbard16":
-        return run_hubbard(args)
+    if args.config in ("xxz28_sectors", "hubbard16"):
+        world, rank, _ = dist_setup()
+        if rank != 0:
+            return 0  # single-GPU workloads: under torchrun only rank 0 runs them
+        return run_sectors(args) if args.config == "xxz28_sectors" else run_hubbard(args)
 
     import torch
 
@@ -573,8 +575,7 @@ def main():
     for _ in range(args.warmup):
         step()
     op.check_errors(sptr)
-    if world > 1:
-        torch.distributed.barrier()
+    rep.barrier()
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
@@ -585,10 +586,7 @@ def main():
         torch.cuda.synchronize()
     op.check_errors(sptr)
     t_ms = start.elapsed_time(end)
-    if world > 1:
-        tt = torch.tensor([t_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_ms = float(tt.item())
+    t_ms = rep.max_over_ranks(t_ms)  # replicas: the slowest rank's time
     ms_per_step = t_ms / args.steps
     value = world * elements * args.steps / (t_ms * 1e-3)
 
