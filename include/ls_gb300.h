@@ -290,6 +290,19 @@ int ls_gpu_check_errors(void *stream);
 /* Number of off-diagonal matrix elements (generated targets found in the basis) of H. */
 int ls_gpu_count_nonzeros(ls_hs_operator const *op, int64_t *nnz);
 
+/* Term application on device batches of basis states, with the results, term order and layout of
+ * ls_internal_operator_apply_diag_x1 / ls_internal_operator_apply_off_diag_x1 (reference.c:67-135,
+ * called by BatchedOperator.chpl:298-357): ys[i] = sum of the real diagonal coefficients of
+ * alphas[i]; off-diagonal targets betas / complex128 coeffs in compressed rows
+ * (offsets[0 .. count], offsets[0] = 0).  betas and coeffs need count * number_off_diag_terms
+ * entries.  Device pointers, stream-ordered; concurrent calls on different streams must not
+ * overlap (they share a scratch buffer). */
+int ls_gpu_operator_apply_diag(ls_hs_operator const *op, int64_t count, uint64_t const *d_alphas,
+                               double *d_ys, void *stream);
+int ls_gpu_operator_apply_off_diag(ls_hs_operator const *op, int64_t count, uint64_t const *d_alphas,
+                                   uint64_t *d_betas, double *d_coeffs, int64_t *d_offsets,
+                                   void *stream);
+
 /* Per-coupling inner products out[c] = <g, H_c x> = sum_i conj(g_i) (H_c x)_i for an operator
  * H = sum_c H_c whose terms are tagged with coupling ids: term_coupling[t] in [0, n_couplings) for
  * the off-diagonal terms, then the diagonal terms, in table order (host array).  g, x: complex128

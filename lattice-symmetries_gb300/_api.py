@@ -285,6 +285,55 @@ class Basis:
         n, _, norms = self._device_info()
         return _DeviceArray(norms, (n,), "<f8", self)
 
+    # -- persistence (the role of the reference's HDF5 basis files, MyHDF5.chpl:255-335) -------
+    def json_object(self) -> dict:
+        raise NotImplementedError
+
+    def save(self, path: str) -> None:
+        """Writes the basis definition and its representatives to `path` (numpy .npz), so that a
+        large basis is enumerated once and loaded afterwards."""
+        import json
+        self.check_is_built()
+        np.savez(path, representatives=np.asarray(self.states, dtype=np.uint64),
+                 definition=np.array(json.dumps(self.json_object())))
+
+    def _set_representatives(self, states: np.ndarray) -> None:
+        """Installs externally stored representatives (ls_hs_unchecked_set_representatives): the
+        array is kept by this object and indexed on the GPU."""
+        if self.is_built:
+            raise ValueError("representatives have already been set")
+        states = np.ascontiguousarray(states, dtype=np.uint64)
+        if len(states) > 1 and not np.all(states[1:] > states[:-1]):
+            raise ValueError("representatives must be sorted and unique")
+        self._loaded_states = states
+        arr = N.chpl_external_array(states.ctypes.data if len(states) else None, len(states), None)
+        self._lib.ls_hs_unchecked_set_representatives(self._payload, byref(arr), 22)
+        N.check()
+
+
+def basis_from_json(obj: dict) -> Basis:
+    """The basis described by Basis.json_object() (not built)."""
+    syms = obj.get("symmetries") or []
+    symmetries = Symmetries([Symmetry(s["permutation"], s["sector"]) for s in syms]) if syms else None
+    particle = obj["particle"]
+    if particle == "spin-1/2":
+        return SpinBasis(obj["number_spins"], obj.get("hamming_weight"), obj.get("spin_inversion"), symmetries)
+    if particle == "spinful-fermion":
+        occ = obj.get("number_particles")
+        return SpinfulFermionBasis(obj["number_sites"], tuple(occ) if isinstance(occ, list) else occ, symmetries)
+    if particle == "spinless-fermion":
+        return SpinlessFermionBasis(obj["number_sites"], obj.get("number_particles"))
+    raise ValueError("unknown particle type: {}".format(particle))
+
+
+def load_basis(path: str) -> Basis:
+    """A basis written by Basis.save, with its representatives installed (no enumeration)."""
+    import json
+    with np.load(path, allow_pickle=False) as f:
+        basis = basis_from_json(json.loads(str(f["definition"])))
+        basis._set_representatives(f["representatives"])
+    return basis
+
 
 def _popcount(x: int) -> int:
     return bin(x).count("1")
@@ -313,6 +362,11 @@ class SpinBasis(Basis):
         self.hamming_weight = hamming_weight
         super().__init__(N.LS_HS_SPIN, n, n, -1 if hamming_weight is None else int(hamming_weight),
                          0 if spin_inversion is None else int(spin_inversion), symmetries)
+
+    def json_object(self) -> dict:
+        inv = int(self._c.spin_inversion)
+        return {"particle": "spin-1/2", "number_spins": self.number_spins, "hamming_weight": self.hamming_weight,
+                "spin_inversion": inv if inv != 0 else None, "symmetries": self.symmetries.json_object()}
 
     def _index_is_identity(self) -> bool:
         return self.hamming_weight is None and self._c.spin_inversion == 0 and self._symmetries.order == 0
@@ -350,6 +404,10 @@ class SpinlessFermionBasis(Basis):
         self.number_particles = number_particles
         super().__init__(N.LS_HS_SPINLESS_FERMION, n,
                          -1 if number_particles is None else int(number_particles), -1, 0, None)
+
+    def json_object(self) -> dict:
+        return {"particle": "spinless-fermion", "number_sites": self.number_sites,
+                "number_particles": self.number_particles}
 
     def _index_is_identity(self) -> bool:
         return self.number_particles is None
@@ -401,6 +459,12 @@ class SpinfulFermionBasis(Basis):
             doubled = symmetries.doubled()
         self.site_symmetries = symmetries
         super().__init__(N.LS_HS_SPINFUL_FERMION, n, total, up, 0, doubled)
+
+    def json_object(self) -> dict:
+        occ = list(self.occupation) if isinstance(self.occupation, tuple) else self.occupation
+        syms = self.site_symmetries.json_object() if self.site_symmetries is not None else []
+        return {"particle": "spinful-fermion", "number_sites": self.number_sites, "number_particles": occ,
+                "symmetries": syms}
 
     def _index_is_identity(self) -> bool:
         return self.occupation is None and (self.site_symmetries is None or self.site_symmetries.order == 0)
@@ -628,6 +692,33 @@ class Operator(_LinearOperator):
         if check:
             N.check(self._lib.ls_gpu_check_errors(stream), "matvec")
         return Y.reshape(D) if squeeze else Y
+
+    def apply_diag_batch(self, alphas):
+        """Diagonal values of device basis states (uint64 / int64 CUDA tensor [B]) -> float64 [B]."""
+        import torch
+        a = alphas.contiguous()
+        ys = torch.empty(a.shape[0], dtype=torch.float64, device=a.device)
+        stream = torch.cuda.current_stream(a.device).cuda_stream
+        N.check(self._lib.ls_gpu_operator_apply_diag(self._payload, a.shape[0], a.data_ptr(), ys.data_ptr(), stream),
+                "apply_diag")
+        return ys
+
+    def apply_off_diag_batch(self, alphas):
+        """Off-diagonal targets of device basis states: (betas int64 [nnz] holding uint64 bit
+        patterns, coeffs complex128 [nnz], offsets int64 [B + 1]), as in the reference's
+        ls_chpl_operator_apply_off_diag."""
+        import torch
+        a = alphas.contiguous()
+        B, T = a.shape[0], max(self.number_off_diag_terms, 0)
+        betas = torch.empty(max(B * T, 1), dtype=torch.int64, device=a.device)
+        coeffs = torch.empty(max(B * T, 1), dtype=torch.complex128, device=a.device)
+        offsets = torch.empty(B + 1, dtype=torch.int64, device=a.device)
+        stream = torch.cuda.current_stream(a.device).cuda_stream
+        N.check(self._lib.ls_gpu_operator_apply_off_diag(self._payload, B, a.data_ptr(), betas.data_ptr(),
+                                                         coeffs.data_ptr(), offsets.data_ptr(), stream),
+                "apply_off_diag")
+        n = int(offsets[-1].item())
+        return betas[:n], coeffs[:n], offsets
 
     def check_errors(self, stream=None):
         import torch

@@ -1332,6 +1332,31 @@ extern "C" int ls_gpu_state_index(ls_hs_basis const* basis, int64_t batch, uint6
   return launch_state_index(ix->dev, batch, d_alphas, d_indices, s);
 }
 
+// BatchedOperator.chpl:298-357 / reference.c:67-135 on device batches (see apply.cu).
+extern "C" int ls_gpu_operator_apply_diag(ls_hs_operator const* op, int64_t count, uint64_t const* d_alphas,
+                                          double* d_ys, void* stream) {
+  if (op == nullptr || count < 0 || (count > 0 && (d_alphas == nullptr || d_ys == nullptr)))
+    return fail(LS_GPU_ERR_INVALID, "invalid arguments");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  OperatorCache* c = operator_cache(op);
+  if (c == nullptr) return LS_GPU_ERR_CUDA;
+  return launch_apply_diag(c->fwd_diag.terms, count, d_alphas, d_ys, (cudaStream_t)stream);
+}
+
+extern "C" int ls_gpu_operator_apply_off_diag(ls_hs_operator const* op, int64_t count, uint64_t const* d_alphas,
+                                              uint64_t* d_betas, double* d_coeffs, int64_t* d_offsets,
+                                              void* stream) {
+  if (op == nullptr || count < 0 || d_offsets == nullptr || (count > 0 && d_alphas == nullptr))
+    return fail(LS_GPU_ERR_INVALID, "invalid arguments");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  OperatorCache* c = operator_cache(op);
+  if (c == nullptr) return LS_GPU_ERR_CUDA;
+  if (c->off.n > 0 && count > 0 && (d_betas == nullptr || d_coeffs == nullptr))
+    return fail(LS_GPU_ERR_INVALID, "betas and coeffs need count * number_off_diag_terms entries");
+  return launch_apply_off_diag(c->fwd_off.terms, count, d_alphas, d_betas, d_coeffs, d_offsets,
+                               (cudaStream_t)stream);
+}
+
 extern "C" int ls_gpu_coupling_inner_products(ls_hs_operator const* op, int n_couplings,
                                               int32_t const* term_coupling, double const* d_g,
                                               double const* d_x, double* d_out, void* stream) {

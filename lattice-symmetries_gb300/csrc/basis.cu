@@ -661,6 +661,10 @@ static int exclusive_scan(const In* d_in, int64_t n, int64_t* d_out, cudaStream_
   return rc;
 }
 
+int exclusive_scan_counts(const int32_t* d_in, int64_t n, int64_t* d_out, cudaStream_t s) {
+  return exclusive_scan<int32_t>(d_in, n, d_out, s);
+}
+
 // ------------------------------------------------------------------------------------------------
 // Enumeration
 // ------------------------------------------------------------------------------------------------

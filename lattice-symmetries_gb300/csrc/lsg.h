@@ -182,6 +182,9 @@ int enumerate_states(const DeviceGroup* g, const EnumerateRequest& req, uint64_t
 int enumerate_states_noalloc(const OrbitData* od, const EnumerateRequest& req, uint64_t* d_out,
                              int64_t capacity, int64_t* count, cudaStream_t s);
 
+// out[i] = sum_{k<i} in[k] for i <= n (out has n + 1 entries); stream-ordered.
+int exclusive_scan_counts(const int32_t* d_in, int64_t n, int64_t* d_out, cudaStream_t s);
+
 int build_prefix_index(const uint64_t* d_reps, int64_t n, int number_bits, int prefix_bits,
                        int64_t** d_offsets, int64_t* range_size, int* shift, cudaStream_t s,
                        uint64_t* max_state);
@@ -221,6 +224,13 @@ int sector_plan_build(const std::vector<MatvecProblem>& problems, bool shareable
 int sector_plan_run(const SectorPlan* plan, int* d_err, cudaStream_t s);
 bool sector_plan_batched(const SectorPlan* plan);
 void sector_plan_free(SectorPlan* plan);
+
+// Per-state term application on device batches (apply.cu), the semantics of
+// ls_internal_operator_apply_{diag,off_diag}_x1 (reference.c:67-135).
+int launch_apply_diag(const DeviceTerms& diag, int64_t count, const uint64_t* d_alphas, double* d_ys,
+                      cudaStream_t s);
+int launch_apply_off_diag(const DeviceTerms& off, int64_t count, const uint64_t* d_alphas, uint64_t* d_betas,
+                          double* d_coeffs, int64_t* d_offsets, cudaStream_t s);
 
 int launch_coupling_products(const MatvecProblem& p, int n_couplings, const double* d_g,
                              const double* d_x, double* d_out, int* d_err, cudaStream_t s);
