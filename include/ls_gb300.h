@@ -236,8 +236,10 @@ void ls_internal_operator_apply_off_diag_x1(ls_hs_operator const *op, ptrdiff_t 
 
 /* Chapel drivers: StatesEnumeration.chpl:692-709, BatchedOperator.chpl:298-357,
  * DistributedMatrixVector.chpl:1090-1105 (chapel/lib/lattice_symmetries_chapel.h:7-41).
- * The matvec reads x and writes y in host memory, numVectors must be 1, exactly as in the
- * reference; complex coefficients contribute their real part (DistributedMatrixVector.chpl:126). */
+ * The matvec reads x and writes y in host memory; complex coefficients contribute their real part
+ * (DistributedMatrixVector.chpl:126).  The reference accepts num_vectors == 1 only; here
+ * num_vectors >= 1 vectors stored one after the other (x[v * D + i], y likewise) share one orbit
+ * scan on the GPU, and num_vectors == 1 behaves exactly as in the reference. */
 void ls_chpl_enumerate_representatives(ls_hs_basis *p, uint64_t lower, uint64_t upper,
                                        chpl_external_array *dest);
 void ls_chpl_operator_apply_diag(ls_hs_operator *matrix, int64_t count, uint64_t *alphas,

@@ -624,6 +624,19 @@ class Operator(_LinearOperator):
         N.check()
         return out
 
+    def apply_to_state_vectors(self, vectors: np.ndarray) -> np.ndarray:
+        """H applied to several real vectors [k, D] (host, float64) in one reference-facing call
+        (ls_chpl_matrix_vector_product with num_vectors = k; one orbit scan for all k)."""
+        self._check_basis_is_built("apply_to_state_vectors")
+        X = np.ascontiguousarray(vectors, dtype=np.float64)
+        if X.ndim != 2 or X.shape[1] != self._basis.number_states:
+            raise ValueError("expected an array of shape [k, {}]".format(self._basis.number_states))
+        Y = np.empty_like(X)
+        self._lib.ls_chpl_matrix_vector_product(self._payload, X.shape[0], N.as_ptr(X, c_double),
+                                                N.as_ptr(Y, c_double))
+        N.check()
+        return Y
+
     def _matvec(self, x):
         x = np.asarray(x)
         if x.ndim == 2:

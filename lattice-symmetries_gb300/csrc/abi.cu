@@ -40,8 +40,8 @@ struct DeviceRuntime {
   int sms = 0;
   int* err_word = nullptr;        // device
   uint64_t* binom = nullptr;      // device 65x65
-  Scratch dev[8];
-  Scratch host[8];
+  Scratch dev[12];
+  Scratch host[12];
 };
 DeviceRuntime g_rt[16];
 
@@ -1122,7 +1122,9 @@ int read_and_clear_error(cudaStream_t s) {
 
 }  // namespace
 
-// DistributedMatrixVector.chpl:1090-1105: y = H x on host arrays, one real vector.
+// DistributedMatrixVector.chpl:1090-1105: y = H x on host arrays.  The reference accepts one real
+// vector; here num_vectors >= 1 vectors stored one after the other (x[v * D + i]) go through one
+// orbit scan (they are transposed on the device to the kernels' [D][k] layout).
 extern "C" void ls_chpl_matrix_vector_product(ls_hs_operator* matrix, int num_vectors, double const* x,
                                               double* y) {
   std::lock_guard<std::mutex> lock(g_mutex);
@@ -1130,8 +1132,8 @@ extern "C" void ls_chpl_matrix_vector_product(ls_hs_operator* matrix, int num_ve
     ls_hs_error("bases with more than 64 bits are not yet implemented");
     return;
   }
-  if (num_vectors != 1) {
-    ls_hs_error("applying the Operator to more than 1 vector is not yet implemented");
+  if (num_vectors < 1) {
+    ls_hs_error("the number of vectors must be positive");
     return;
   }
   MatvecProblem p;
@@ -1141,17 +1143,23 @@ extern "C" void ls_chpl_matrix_vector_product(ls_hs_operator* matrix, int num_ve
     return;
   }
   const int64_t n = p.n_rows;
+  const int k = num_vectors;
   cudaStream_t s = default_stream();
-  double* d_x = (double*)scratch((size_t)std::max<int64_t>(n, 1) * 8, 4);
-  double* d_y = (double*)scratch((size_t)std::max<int64_t>(n, 1) * 8, 5);
-  if (!d_x || !d_y) {
+  const size_t bytes = (size_t)std::max<int64_t>(n, 1) * k * 8;
+  double* d_x = (double*)scratch(bytes, 4);
+  double* d_y = (double*)scratch(bytes, 5);
+  double* d_xt = k > 1 ? (double*)scratch(bytes, 8) : d_x;
+  double* d_yt = k > 1 ? (double*)scratch(bytes, 9) : d_y;
+  if (!d_x || !d_y || !d_xt || !d_yt) {
     report("ls_chpl_matrix_vector_product");
     return;
   }
   if (n > 0) {
-    if (!cuda_ok(cudaMemcpyAsync(d_x, x, (size_t)n * 8, cudaMemcpyHostToDevice, s), "H2D x")) rc = LS_GPU_ERR_CUDA;
-    if (rc == 0) rc = launch_matvec(p, Scalar::Real, 1, d_x, 1, d_y, 1, device_error_word(), s);
-    if (rc == 0 && !cuda_ok(cudaMemcpyAsync(y, d_y, (size_t)n * 8, cudaMemcpyDeviceToHost, s), "D2H y"))
+    if (!cuda_ok(cudaMemcpyAsync(d_x, x, (size_t)n * k * 8, cudaMemcpyHostToDevice, s), "H2D x")) rc = LS_GPU_ERR_CUDA;
+    if (rc == 0 && k > 1) rc = launch_transpose(d_x, d_xt, k, n, s);
+    if (rc == 0) rc = launch_matvec(p, Scalar::Real, k, d_xt, k, d_yt, k, device_error_word(), s);
+    if (rc == 0 && k > 1) rc = launch_transpose(d_yt, d_y, n, k, s);
+    if (rc == 0 && !cuda_ok(cudaMemcpyAsync(y, d_y, (size_t)n * k * 8, cudaMemcpyDeviceToHost, s), "D2H y"))
       rc = LS_GPU_ERR_CUDA;
     if (rc == 0) rc = read_and_clear_error(s);
   }

@@ -82,4 +82,19 @@ int launch_apply_off_diag(const DeviceTerms& off, int64_t count, const uint64_t*
   return cuda_ok(cudaGetLastError(), "k_apply_write") ? 0 : LS_GPU_ERR_CUDA;
 }
 
+// out[c][r] = in[r][c] for an in matrix of rows x cols doubles (row-major).
+__global__ void k_transpose(const double* __restrict__ in, double* __restrict__ out, int64_t rows, int64_t cols) {
+  const int64_t total = rows * cols;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / cols, c = e - r * cols;
+    out[c * rows + r] = in[e];
+  }
+}
+
+int launch_transpose(const double* d_in, double* d_out, int64_t rows, int64_t cols, cudaStream_t s) {
+  if (rows * cols == 0) return 0;
+  k_transpose<<<blocks_for(rows * cols), 256, 0, s>>>(d_in, d_out, rows, cols);
+  return cuda_ok(cudaGetLastError(), "k_transpose") ? 0 : LS_GPU_ERR_CUDA;
+}
+
 }  // namespace lsg

@@ -232,6 +232,9 @@ int launch_apply_diag(const DeviceTerms& diag, int64_t count, const uint64_t* d_
 int launch_apply_off_diag(const DeviceTerms& off, int64_t count, const uint64_t* d_alphas, uint64_t* d_betas,
                           double* d_coeffs, int64_t* d_offsets, cudaStream_t s);
 
+// out = in^T for a row-major rows x cols matrix of doubles (apply.cu).
+int launch_transpose(const double* d_in, double* d_out, int64_t rows, int64_t cols, cudaStream_t s);
+
 int launch_coupling_products(const MatvecProblem& p, int n_couplings, const double* d_g,
                              const double* d_x, double* d_out, int* d_err, cudaStream_t s);
 

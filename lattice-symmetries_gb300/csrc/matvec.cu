@@ -14,8 +14,14 @@ int launch_packed(bool cplx, int k, int gpl, bool inv, const MatvecProblem& p, c
     return launch_packed_fermi(cplx, k, gpl, p, L, sh, x, ldx, y, ldy, err, binom, s);
   }
   if (!cplx) {
-    if (k != 1) return LS_GPU_ERR_INVALID;
-    return launch_packed_real(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
+    switch (k) {
+      case 1: return launch_packed_real(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
+      case 2: return launch_packed_real_k2(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
+      case 4: return launch_packed_real_k4(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
+      case 8: return launch_packed_real_k8(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
+      case 16: return launch_packed_real_k16(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
+      default: return LS_GPU_ERR_INVALID;
+    }
   }
   switch (k) {
     case 1: return launch_packed_cplx_k1(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
@@ -67,8 +73,9 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
       int done = 0;
       while (done < k) {
         const int left = k - done;
-        int chunk = 1;
-        if (cplx) chunk = left >= 16 ? 16 : left >= 8 ? 8 : left >= 4 ? 4 : 1;
+        int chunk = left >= 16 ? 16 : left >= 8 ? 8 : left >= 4 ? 4 : 1;
+        if (!cplx && left == 2) chunk = 2;
+        if (p.group.fermionic && !cplx) chunk = 1;  // fermionic real path: one column per launch
         const double* xs = d_x + (size_t)done * scalar_words;
         double* ys = d_y + (size_t)done * scalar_words;
         int rc = launch_packed(cplx, chunk, p.group.gpl, inv, p, PL, sh, xs, ldx, ys, ldy, d_err, binom, s);

@@ -28,6 +28,10 @@ int launch_packed(bool cplx, int k, int gpl, bool inv, const MatvecProblem& p, c
            const double* x, int64_t ldx, double* y, int64_t ldy, int* err, const uint64_t* binom, \
            cudaStream_t s);
 LSG_DECLARE_PACKED(launch_packed_real)
+LSG_DECLARE_PACKED(launch_packed_real_k2)
+LSG_DECLARE_PACKED(launch_packed_real_k4)
+LSG_DECLARE_PACKED(launch_packed_real_k8)
+LSG_DECLARE_PACKED(launch_packed_real_k16)
 LSG_DECLARE_PACKED(launch_packed_cplx_k1)
 LSG_DECLARE_PACKED(launch_packed_cplx_k4)
 LSG_DECLARE_PACKED(launch_packed_cplx_k8)

@@ -65,3 +65,16 @@ def test_empty_batch():
     op = ls.Operator(ls.SpinBasis(8), LAT.heisenberg(LAT.chain_bonds(8)))
     b, c, o = op.apply_off_diag_batch(torch.zeros(0, dtype=torch.int64, device="cuda"))
     assert o.shape == (1,) and int(o[0]) == 0 and b.numel() == 0
+
+
+@pytest.mark.parametrize("k", [2, 3, 5, 16])
+def test_reference_call_with_several_vectors(k):
+    """ls_chpl_matrix_vector_product with num_vectors = k equals k one-vector calls."""
+    from ls_helpers import chain_case, square_case
+    for case in (chain_case(16, 0, 0, 1), chain_case(16, 3), square_case(4, 2, 2, 1, J2=0.5)):
+        case.basis.build()
+        D = case.basis.number_states
+        X = np.random.default_rng(k).normal(size=(k, D))
+        Y = case.op.apply_to_state_vectors(X)
+        ref = np.stack([case.op.apply_to_state_vector(X[v].copy()) for v in range(k)])
+        assert np.abs(Y - ref).max() <= 1e-13 * np.abs(ref).max()
