@@ -1103,6 +1103,15 @@ int make_problem(ls_hs_operator const* op, bool adjoint, MatvecProblem* p) {
   p->diag = adjoint ? c->adj_diag.terms : c->fwd_diag.terms;
   p->off.coupling = p->diag.coupling = c->d_coupling;
   p->n_rows = ix->n_states;
+  // Real matrix elements: real term coefficients and real characters.  Characters are
+  // cos/sin(-2 pi phi) in floating point (Group.hs:115-116), so sectors such as (pi, pi) carry
+  // imaginary parts of order 1e-16; below 1e-14 they are treated as zero here (the dropped terms
+  // are below 1e-15 of the result).
+  bool real = true;
+  for (int t = 0; t < c->off.n && real; ++t) real = c->off.v[2 * t + 1] == 0.0;
+  if (p->projection == 2 && od != nullptr)
+    for (int e = 0; e < od->n_elems && real; ++e) real = std::fabs(od->chars_im[e]) <= 1e-14;
+  p->real_elements = real ? 1 : 0;
   return 0;
 }
 

@@ -207,6 +207,9 @@ struct MatvecProblem {
   DeviceTerms diag;
   int64_t n_rows;
   unsigned long long* nnz_counter = nullptr;  // optional: counts off-diagonal elements found
+  // Every off-diagonal matrix element is real (real term coefficients and real characters): a
+  // complex right-hand side then needs 2 FP64 FMAs per element instead of 4.
+  int real_elements = 0;
 };
 
 int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, int64_t ldx,

@@ -148,6 +148,7 @@ int sector_plan_build(const std::vector<MatvecProblem>& problems, bool shareable
                   p0.group.gpl <= kSectorMaxGpl && p0.group.onehot_packed != nullptr;
   if (plan->batched) {
     plan->shared = p0;
+    for (const MatvecProblem& q : problems) plan->shared.real_elements &= q.real_elements;
     plan->layout = make_packed_layout(p0, n);
     if (plan->layout.total > kMaxDynamicSmem) plan->batched = false;
   }

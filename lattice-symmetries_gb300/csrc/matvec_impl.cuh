@@ -484,7 +484,7 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
                                            const int64_t ldx, double* __restrict__ y, const int64_t ldy,
                                            const int64_t row, int* __restrict__ err,
                                            const uint64_t* __restrict__ binom,
-                                           unsigned long long* nnz_counter) {
+                                           unsigned long long* nnz_counter, const bool real_elements) {
   constexpr unsigned FULL = 0xffffffffu;
   constexpr int Gp = 32 * GPL;
   constexpr int Q = 32 / K;
@@ -561,6 +561,22 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
         fre = f.re * nj;
         fim = f.im * nj;
       }
+    }
+    if (CPLX && real_elements) {
+      // real matrix elements (warp-uniform branch): complex x times a real factor
+      for (int s0 = 0; s0 < nslot; s0 += Q) {
+        const int s = s0 + q;
+        const int src = s & 31;
+        const int64_t js = (K == 1) ? j : __shfl_sync(FULL, j, src);
+        const double sre = (K == 1) ? fre : __shfl_sync(FULL, fre, src);
+        if (s < nslot && js >= 0) {
+          const double2 xv = __ldg(reinterpret_cast<const double2*>(x) + js * ldx + rhs);
+          acc.re += sre * xv.x;
+          acc.im += sre * xv.y;
+        }
+        if (K == 1) break;
+      }
+      return;
     }
     for (int s0 = 0; s0 < nslot; s0 += Q) {
       const int s = s0 + q;
@@ -682,7 +698,7 @@ __global__ void __launch_bounds__(320, 2)
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t row = warp_id; row < p.n_rows; row += n_warps)
     packed_row<GPL, INV, CPLX, K, FERMI>(T, p.group.n_bits, p.index, T.ch, p.group.spin_inversion, p.constraint, x, ldx,
-                                  y, ldy, row, err, binom, p.nnz_counter);
+                                  y, ldy, row, err, binom, p.nnz_counter, p.real_elements != 0);
 }
 
 // Batched kernel: the rows of all sectors form one row space that a persistent grid walks; each
@@ -713,7 +729,7 @@ __global__ void __launch_bounds__(320, 2)
     }
     const SectorDesc& S = sd[lo];
     packed_row<GPL, INV, true, K>(T, p.group.n_bits, S.index, S.chars, (int)S.spin_inversion, p.constraint, S.x,
-                                  ldx, S.y, ldy, row - S.row_begin, err, binom, p.nnz_counter);
+                                  ldx, S.y, ldy, row - S.row_begin, err, binom, p.nnz_counter, p.real_elements != 0);
   }
 }
 
