@@ -391,8 +391,12 @@ int ls_gpu_enumerate_noalloc(ls_hs_basis const *basis, uint64_t *d_out, int64_t 
 /* Tuning knobs of the projected matvec kernels: threads per CTA (256 or 320) and grid waves (the
  * grid is 2 * SMs * waves CTAs, one warp per row at a time); 0 = default (256, 4). */
 int ls_gpu_set_matvec_config(int threads_per_block, int waves);
+/* Most right-hand sides per kernel launch (16, 8, 4 or 1; larger k is split into launches). */
+int ls_gpu_set_matvec_rhs_tile(int rhs_tile);
+int ls_gpu_get_matvec_config(int *threads_per_block, int *waves, int *rhs_tile);
 /* Autotuner: times the matvec of `op` on k complex right-hand sides over a table of
- * (threads, waves) pairs and installs the fastest; reports it and its time (ms). */
+ * (threads, waves) pairs and, for k >= 8, right-hand-side tiles, and installs the fastest;
+ * reports the launch shape and its time (ms). */
 int ls_gpu_autotune_matvec(ls_hs_operator const *op, int k, int *best_threads, int *best_waves,
                            double *best_ms);
 

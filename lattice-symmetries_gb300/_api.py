@@ -740,12 +740,19 @@ class Operator(_LinearOperator):
         N.check(self._lib.ls_gpu_check_errors(stream), "matvec")
 
     def autotune(self, k: int = 1):
-        """Times the GPU matvec over (threads per block, grid waves) and installs the fastest.
-        Returns (threads, waves, milliseconds)."""
+        """Times the GPU matvec over (threads per block, grid waves) and, for k >= 8, the
+        right-hand-side tile, and installs the fastest.  Returns (threads, waves, milliseconds)."""
         th, wv, ms = ctypes.c_int(0), ctypes.c_int(0), c_double(0.0)
         N.check(self._lib.ls_gpu_autotune_matvec(self._payload, int(k), byref(th), byref(wv), byref(ms)),
                 "autotune")
         return th.value, wv.value, ms.value
+
+    @staticmethod
+    def launch_config():
+        """(threads per block, grid waves, right-hand-side tile) used by the matvec kernels."""
+        th, wv, tile = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        N.lib().ls_gpu_get_matvec_config(byref(th), byref(wv), byref(tile))
+        return th.value, wv.value, tile.value
 
     def count_nonzeros(self) -> int:
         """Off-diagonal matrix elements of H in this basis (generated targets found in the basis)."""

@@ -174,6 +174,8 @@ _SIGNATURES = [
     ("ls_gpu_is_representative", c_int, [POINTER(ls_hs_basis), c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("ls_gpu_state_index", c_int, [POINTER(ls_hs_basis), c_int64, c_void_p, c_void_p, c_void_p]),
     ("ls_gpu_set_matvec_config", c_int, [c_int, c_int]),
+    ("ls_gpu_set_matvec_rhs_tile", c_int, [c_int]),
+    ("ls_gpu_get_matvec_config", c_int, [POINTER(c_int), POINTER(c_int), POINTER(c_int)]),
     ("ls_gpu_check_errors", c_int, [c_void_p]),
     ("ls_gpu_enumerate_noalloc", c_int, [POINTER(ls_hs_basis), c_void_p, c_int64, POINTER(c_int64), c_void_p]),
     ("ls_gpu_autotune_matvec", c_int, [POINTER(ls_hs_operator), c_int, POINTER(c_int), POINTER(c_int),

@@ -17,6 +17,8 @@
 
 namespace lsg {
 int set_matvec_config(int threads, int blocks_per_sm);
+int set_matvec_rhs_tile(int tile);
+void get_matvec_config(int* threads, int* waves, int* rhs_tile);
 }
 
 using namespace lsg;
@@ -235,6 +237,18 @@ extern "C" void ls_chpl_finalize(void) {
 
 extern "C" int ls_gpu_device_synchronize(void) {
   return cuda_ok(cudaStreamSynchronize(default_stream()), "synchronize") ? 0 : LS_GPU_ERR_CUDA;
+}
+
+extern "C" int ls_gpu_set_matvec_rhs_tile(int rhs_tile) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  const int rc = set_matvec_rhs_tile(rhs_tile);
+  return rc != 0 ? fail(rc, "the right-hand-side tile must be 1, 4, 8 or 16") : 0;
+}
+
+extern "C" int ls_gpu_get_matvec_config(int* threads_per_block, int* waves, int* rhs_tile) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  get_matvec_config(threads_per_block, waves, rhs_tile);
+  return 0;
 }
 
 extern "C" int ls_gpu_set_matvec_config(int threads_per_block, int blocks_per_sm) {
@@ -1255,12 +1269,35 @@ extern "C" int ls_gpu_autotune_matvec(ls_hs_operator const* op, int k, int* best
     }
     if (rc != 0) break;
   }
+  set_matvec_config(bt, bw);
+  // right-hand-side tile: for k >= 8, one launch of 16 columns against two of 8 (or four of 4)
+  int btile = 16;
+  if (rc == 0 && k >= 8) {
+    double tbest = 1e300;
+    for (int tile : {16, 8, 4}) {
+      if (tile > k && tile != 4) continue;
+      set_matvec_rhs_tile(tile);
+      rc = gpu_matvec(op, Scalar::Complex, k, d_x, k, d_y, k, 0, s);
+      if (rc != 0) break;
+      cudaEventRecord(e0, s);
+      rc = gpu_matvec(op, Scalar::Complex, k, d_x, k, d_y, k, 0, s);
+      cudaEventRecord(e1, s);
+      if (rc != 0 || !cuda_ok(cudaEventSynchronize(e1), "autotune")) break;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < tbest) {
+        tbest = ms;
+        btile = tile;
+      }
+    }
+    if (tbest < best) best = tbest;
+  }
+  set_matvec_rhs_tile(btile);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(d_x);
   cudaFree(d_y);
   if (rc == 0) rc = ls_gpu_check_errors(s);
-  set_matvec_config(bt, bw);
   if (best_threads) *best_threads = bt;
   if (best_waves) *best_waves = bw;
   if (best_ms) *best_ms = best;

@@ -34,11 +34,24 @@ int launch_packed(bool cplx, int k, int gpl, bool inv, const MatvecProblem& p, c
 
 static int g_threads_override = 0;
 static int g_blocks_per_sm_override = 0;
+static int g_rhs_tile = 16;  // most right-hand sides per launch (16, 8, 4 or 1)
 
 int set_matvec_config(int threads, int blocks_per_sm) {
   g_threads_override = threads;
   g_blocks_per_sm_override = blocks_per_sm;
   return 0;
+}
+
+int set_matvec_rhs_tile(int tile) {
+  if (tile != 1 && tile != 4 && tile != 8 && tile != 16) return LS_GPU_ERR_INVALID;
+  g_rhs_tile = tile;
+  return 0;
+}
+
+void get_matvec_config(int* threads, int* waves, int* rhs_tile) {
+  if (threads) *threads = g_threads_override > 0 ? g_threads_override : 320;
+  if (waves) *waves = g_blocks_per_sm_override > 0 ? g_blocks_per_sm_override : 8;
+  if (rhs_tile) *rhs_tile = g_rhs_tile;
 }
 
 extern const uint64_t* device_binomials();
@@ -73,8 +86,9 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
       int done = 0;
       while (done < k) {
         const int left = k - done;
-        int chunk = left >= 16 ? 16 : left >= 8 ? 8 : left >= 4 ? 4 : 1;
-        if (!cplx && left == 2) chunk = 2;
+        const int most = std::min(left, g_rhs_tile);
+        int chunk = most >= 16 ? 16 : most >= 8 ? 8 : most >= 4 ? 4 : 1;
+        if (!cplx && left == 2 && g_rhs_tile >= 2) chunk = 2;
         if (p.group.fermionic && !cplx) chunk = 1;  // fermionic real path: one column per launch
         const double* xs = d_x + (size_t)done * scalar_words;
         double* ys = d_y + (size_t)done * scalar_words;
