@@ -162,7 +162,6 @@ int sector_plan_build(const std::vector<MatvecProblem>& problems, bool shareable
                   p0.group.gpl <= kSectorMaxGpl && p0.group.onehot_packed != nullptr;
   if (plan->batched) {
     plan->shared = p0;
-    for (const MatvecProblem& q : problems) plan->shared.real_elements &= q.real_elements;
     plan->layout = make_packed_layout(p0, n);
     if (plan->layout.total > kMaxDynamicSmem) plan->batched = false;
   }
@@ -174,6 +173,7 @@ int sector_plan_build(const std::vector<MatvecProblem>& problems, bool shareable
       h[i].chars = problems[i].group.chars_packed;
       h[i].row_begin = rows;
       h[i].spin_inversion = problems[i].group.spin_inversion;
+      h[i].real_elements = problems[i].real_elements;
       rows += problems[i].n_rows;
     }
     plan->total_rows = rows;

@@ -390,6 +390,7 @@ struct SectorDesc {
   double* y;
   int64_t row_begin;     // first row of the sector in the batch's concatenated row space
   int64_t spin_inversion;
+  int64_t real_elements; // every matrix element of this sector is real
 };
 static_assert(sizeof(SectorDesc) % 8 == 0, "sector descriptors are staged as 64-bit words");
 
@@ -729,7 +730,7 @@ __global__ void __launch_bounds__(320, 2)
     }
     const SectorDesc& S = sd[lo];
     packed_row<GPL, INV, true, K>(T, p.group.n_bits, S.index, S.chars, (int)S.spin_inversion, p.constraint, S.x,
-                                  ldx, S.y, ldy, row - S.row_begin, err, binom, p.nnz_counter, p.real_elements != 0);
+                                  ldx, S.y, ldy, row - S.row_begin, err, binom, p.nnz_counter, S.real_elements != 0);
   }
 }
 

@@ -43,7 +43,7 @@ def _gram(X, Y, blocks: int = 256, min_rows: int = 64):
     return main + X[:, c * m:].mH @ Y[:, c * m:]
 
 
-def _cholqr(W, eps: float = 1e-15):
+def _cholqr(W, eps: float = 1e-15, passes: int = 2):
     """W = Q R with Q orthonormal (batched over the leading dimension): two Cholesky-QR passes.
     A tiny diagonal shift keeps exhausted blocks (W ~ 0) finite instead of NaN.  The k x k factor
     is inverted explicitly, so that applying it is a GEMM rather than a triangular solve over D."""
@@ -53,7 +53,7 @@ def _cholqr(W, eps: float = 1e-15):
     eye = torch.eye(k, dtype=W.dtype, device=W.device)
     R = None
     Q = W
-    for _ in range(2):
+    for _ in range(passes):
         G = _gram(Q, Q)
         G = 0.5 * (G + G.mH)
         scale = torch.diagonal(G, dim1=-2, dim2=-1).real.mean(-1).clamp_min(1e-300)
@@ -66,23 +66,24 @@ def _cholqr(W, eps: float = 1e-15):
     return Q, R
 
 
-def lanczos_step(apply: Callable[[], None], Q, W, Qp, Bp, A_out, B_out) -> None:
+def lanczos_step(apply: Callable[[], None], Q, W, Qp, Bp, A_out, B_out, lean: bool = False) -> None:
     """One block-Lanczos step on preallocated tensors ([S, D, k] blocks, [S, k, k] coefficients).
 
     `apply()` must compute W = H Q in place.  On return Q holds Q_{j+1}, Qp holds Q_j,
     Bp = B_out = B_j and A_out = A_j.  Everything is stream-ordered (no host synchronisation), so
-    the step can be captured in a CUDA graph."""
-    import torch
-
+    the step can be captured in a CUDA graph.  lean=True skips the local re-orthogonalisation
+    and uses one Cholesky-QR pass: 5 tall-skinny products per step instead of 9 (they are FP64
+    bound on GB300)."""
     apply()
     A = _gram(Q, W)
     W.baddbmm_(Q, A, beta=1.0, alpha=-1.0)
     W.baddbmm_(Qp, Bp.mH, beta=1.0, alpha=-1.0)
-    C = _gram(Q, W)  # local re-orthogonalisation against the current block
-    W.baddbmm_(Q, C, beta=1.0, alpha=-1.0)
-    A = A + C
+    if not lean:
+        C = _gram(Q, W)  # local re-orthogonalisation against the current block
+        W.baddbmm_(Q, C, beta=1.0, alpha=-1.0)
+        A = A + C
     A = 0.5 * (A + A.mH)
-    Qn, B = _cholqr(W)
+    Qn, B = _cholqr(W, passes=1 if lean else 2)
     Qp.copy_(Q)
     Q.copy_(Qn)
     Bp.copy_(B)
@@ -106,7 +107,7 @@ def block_tridiagonal(A: List, B: List):
 
 
 def block_lanczos(apply: Callable[[], None], Q, W, steps: int, graph: bool = False,
-                  timer: Optional[dict] = None):
+                  timer: Optional[dict] = None, lean: bool = False):
     """Runs `steps` block-Lanczos steps with W = H Q computed by `apply()`; Q must hold an
     orthonormal starting block.  Returns the eigenvalues of T per sector ([S, steps * k],
     ascending).  With graph=True one step is captured in a CUDA graph after a warm-up step
@@ -130,12 +131,12 @@ def block_lanczos(apply: Callable[[], None], Q, W, steps: int, graph: bool = Fal
         side = torch.cuda.Stream(Q.device)
         side.wait_stream(torch.cuda.current_stream(Q.device))
         with torch.cuda.stream(side):
-            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur)  # step 0, also the warm-up
+            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur, lean)  # step 0, also the warm-up
         torch.cuda.current_stream(Q.device).wait_stream(side)
         record()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
-            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur)
+            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur, lean)
         # capture does not execute: step 1 runs at the first replay below
     start = end = None
     if timer is not None and Q.is_cuda:
@@ -148,7 +149,7 @@ def block_lanczos(apply: Callable[[], None], Q, W, steps: int, graph: bool = Fal
         if g is not None:
             g.replay()
         else:
-            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur)
+            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur, lean)
         record()
     if start is not None:
         end.record()
@@ -176,10 +177,10 @@ def random_start(batch, seed: int = 0):
 
 
 def sector_ground_states(batch, steps: int, seed: int = 0, graph: bool = True,
-                         timer: Optional[dict] = None) -> np.ndarray:
+                         timer: Optional[dict] = None, lean: bool = False) -> np.ndarray:
     """Lowest eigenvalue of every sector of a SectorBatch after `steps` block-Lanczos steps."""
     random_start(batch, seed)
-    ev = block_lanczos(lambda: batch.run(), batch.X, batch.Y, steps, graph=graph, timer=timer)
+    ev = block_lanczos(lambda: batch.run(), batch.X, batch.Y, steps, graph=graph, timer=timer, lean=lean)
     batch.check_errors()
     return ev[:, 0].cpu().numpy()
 

@@ -78,3 +78,15 @@ def test_ground_state_ritz_vector():
     assert abs(e0 - float(ref)) < 1e-9
     r = H[0] @ psi - e0 * psi
     assert float(torch.linalg.vector_norm(r)) < 1e-6
+
+
+def test_lean_steps_reach_the_same_extremal_eigenvalues():
+    H = random_hermitian(2, 60, seed=21)
+    ref = torch.linalg.eigvalsh(H)
+    for lean in (False, True):
+        g = torch.Generator().manual_seed(9)
+        Q = torch.randn((2, 60, 4), generator=g, dtype=torch.float64).to(torch.complex128)
+        Q, _ = lanczos._cholqr(Q)
+        W = torch.empty_like(Q)
+        ev = lanczos.block_lanczos(lambda: W.copy_(H @ Q), Q, W, 14, lean=lean)
+        assert float((ev[:, 0] - ref[:, 0]).abs().max()) < 1e-8
