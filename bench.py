@@ -503,7 +503,7 @@ def run_sectors(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
         "config": {"workload": args.config, "description": c["description"], "sectors": len(ops),
                    "states": sum(sizes), "nnz": sum(nnzs), "rhs": k, "parallelism": "replicas",
-                   "l2": "inputs larger than L2 (X, Y 10 GB each)"},
+                   "l2": "inputs larger than L2 (X, Y {:.2f} GB each)".format(batch.X.numel() * 16 / 1e9)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_source": peak_kind, "bytes_per_launch": bytes_per_launch},
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps, "clocks": clocks.summary(),

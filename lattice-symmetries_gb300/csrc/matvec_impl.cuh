@@ -722,13 +722,17 @@ __global__ void __launch_bounds__(320, 2)
   __syncthreads();
   const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int cur = 0;  // sector of the previous row: a warp's rows stay in one sector for many steps
   for (int64_t row = warp_id; row < total_rows; row += n_warps) {
-    int lo = 0, hi = n_sectors - 1;  // last sector with row_begin <= row
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (sd[mid].row_begin <= row) lo = mid; else hi = mid - 1;
+    if (row < sd[cur].row_begin || (cur + 1 < n_sectors && row >= sd[cur + 1].row_begin)) {
+      int lo = 0, hi = n_sectors - 1;  // last sector with row_begin <= row
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sd[mid].row_begin <= row) lo = mid; else hi = mid - 1;
+      }
+      cur = lo;
     }
-    const SectorDesc& S = sd[lo];
+    const SectorDesc& S = sd[cur];
     packed_row<GPL, INV, true, K>(T, p.group.n_bits, S.index, S.chars, (int)S.spin_inversion, p.constraint, S.x,
                                   ldx, S.y, ldy, row - S.row_begin, err, binom, p.nnz_counter, S.real_elements != 0);
   }
