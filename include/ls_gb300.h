@@ -292,6 +292,10 @@ int ls_gpu_check_errors(void *stream);
 /* Number of off-diagonal matrix elements (generated targets found in the basis) of H. */
 int ls_gpu_count_nonzeros(ls_hs_operator const *op, int64_t *nnz);
 
+/* Releases the device copies of an operator's term tables (made on the first GPU use of `op`,
+ * keyed by its address).  Call before freeing or reusing the ls_hs_operator; no-op otherwise. */
+void ls_gpu_release_operator(ls_hs_operator const *op);
+
 /* Term application on device batches of basis states, with the results, term order and layout of
  * ls_internal_operator_apply_diag_x1 / ls_internal_operator_apply_off_diag_x1 (reference.c:67-135,
  * called by BatchedOperator.chpl:298-357): ys[i] = sum of the real diagonal coefficients of

@@ -554,6 +554,13 @@ class Operator(_LinearOperator):
     def _payload(self):
         return ctypes.pointer(self._c)
 
+    def __del__(self):
+        try:
+            if getattr(self, "_c", None) is not None:
+                self._lib.ls_gpu_release_operator(ctypes.pointer(self._c))
+        except Exception:
+            pass
+
     @property
     def basis(self) -> Basis:
         return self._basis

@@ -165,6 +165,7 @@ _SIGNATURES = [
                                           c_int64, POINTER(c_void_p), c_int64, c_int, POINTER(c_void_p)]),
     ("ls_gpu_sector_plan_run", c_int, [c_void_p, c_void_p]),
     ("ls_gpu_set_enumeration_rule", c_int, [c_int]),
+    ("ls_gpu_release_operator", None, [POINTER(ls_hs_operator)]),
     ("ls_gpu_operator_apply_diag", c_int, [POINTER(ls_hs_operator), c_int64, c_void_p, c_void_p, c_void_p]),
     ("ls_gpu_operator_apply_off_diag", c_int, [POINTER(ls_hs_operator), c_int64, c_void_p, c_void_p, c_void_p,
                                                c_void_p, c_void_p]),

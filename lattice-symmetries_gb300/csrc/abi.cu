@@ -1386,6 +1386,17 @@ extern "C" int ls_gpu_state_index(ls_hs_basis const* basis, int64_t batch, uint6
   return launch_state_index(ix->dev, batch, d_alphas, d_indices, s);
 }
 
+// Frees the device copies of an operator's term tables (uploaded on first use, keyed by the
+// ls_hs_operator address).  Call it before the operator's memory is released or reused; sector
+// plans that use the operator fail to run afterwards instead of reading freed tables.
+extern "C" void ls_gpu_release_operator(ls_hs_operator const* op) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  auto it = g_ops.find(op);
+  if (it == g_ops.end()) return;
+  free_cache(it->second);
+  g_ops.erase(it);
+}
+
 // BatchedOperator.chpl:298-357 / reference.c:67-135 on device batches (see apply.cu).
 extern "C" int ls_gpu_operator_apply_diag(ls_hs_operator const* op, int64_t count, uint64_t const* d_alphas,
                                           double* d_ys, void* stream) {
