@@ -50,6 +50,11 @@ CONFIGS = {
                       description="Hubbard 4x4 torus, t=1, U=8, 7 up + 7 down, translations x C4v with "
                                   "fermionic signs, Gamma sector; 8 complex RHS, block Lanczos ground state and "
                                   "dE0/d(t, U) by Hellmann-Feynman vs finite differences"),
+    "ladder28_grad": dict(rungs=14, theta=(1.0, 0.7, 0.2), seed=4,
+                          description="2-leg spin-1/2 ladder, 14 rungs PBC along legs, couplings J_leg, J_rung, "
+                                      "D (z.(S_i x S_j) along legs), theta=(1.0, 0.7, 0.2), leg translations x leg "
+                                      "exchange, Sz=0, k=0; loss Re<v, H(theta) x>, backward = adjoint matvec + "
+                                      "per-coupling products, checked against central differences (h=1e-6)"),
     "xxz24_sectors": dict(n=24, delta=1.5, rhs=16, lanczos_steps=100, seed=3,
                           description="XXZ chain N=24 PBC, Delta=1.5, Sz=0, 24 momenta x z=+-1 (48 sectors), "
                                       "16 RHS: the batched workload at a size for kernel profiles"),
@@ -274,6 +279,98 @@ def run_reference(args):
                          "sample": "first {} of {} columns per step (scatter form, oracle/ls_oracle.c); setup: {} ({:.1f} s)".format(
                              cols, D, setup, t_build)},
         "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ladder(args):
+    """Differentiation workload: forward y = H(theta) x and the hand-written backward (adjoint
+    matvec for dL/dx, fused per-coupling products for dL/dtheta), with a central-difference check."""
+    import torch
+
+    ls = importlib.import_module("lattice-symmetries_gb300")
+    lat = importlib.import_module("lattice-symmetries_gb300.lattices")
+    ag = importlib.import_module("lattice-symmetries_gb300.autograd")
+    c = CONFIGS[args.config]
+    R = c["rungs"]
+    torch.cuda.set_device(0)
+    legs, rungs = lat.ladder(R)
+    basis = ls.SpinBasis(2 * R, R, None, ls.Symmetries(lat.ladder_symmetries(R, 0, 0)))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    basis.build()
+    t_build = time.perf_counter() - t0
+    parts = [lat.heisenberg(legs, 0.25), lat.heisenberg(rungs, 0.25), lat.dm_z(legs, 1.0)]
+    theta0 = list(c["theta"])
+    pop = ag.ParametrizedOperator(basis, parts, theta=theta0)
+    D = basis.number_states
+    nnz = pop.operator.count_nonzeros()
+    elements = D + nnz
+    rng = np.random.default_rng(c["seed"])
+    v = torch.from_numpy(rng.normal(size=D) + 1j * rng.normal(size=D)).cuda()
+    x0 = torch.from_numpy(rng.normal(size=D) + 1j * rng.normal(size=D)).cuda()
+    stream = torch.cuda.current_stream()
+
+    def forward_backward():
+        theta = torch.tensor(theta0, dtype=torch.float64, requires_grad=True)
+        x = x0.clone().requires_grad_(True)
+        loss = torch.real(torch.vdot(v, pop.apply(theta, x)))
+        loss.backward()
+        return loss, theta.grad, x.grad
+
+    for _ in range(args.warmup):
+        forward_backward()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clocks:
+        start.record(stream)
+        for _ in range(args.steps):
+            loss, gtheta, gx = forward_backward()
+        end.record(stream)
+        torch.cuda.synchronize()
+    t_ms = start.elapsed_time(end) / args.steps
+    # a forward + backward step touches every matrix element three times: H x, H^dagger v and the
+    # per-coupling products <v, H_c x>
+    value = 3 * elements / (t_ms * 1e-3)
+    # parts of the step
+    start.record(stream)
+    y = pop.operator.apply_device(x0, check=False)
+    end.record(stream)
+    torch.cuda.synchronize()
+    t_fwd = start.elapsed_time(end)
+    start.record(stream)
+    pop.operator.apply_device(v, adjoint=True, check=False)
+    end.record(stream)
+    torch.cuda.synchronize()
+    t_adj = start.elapsed_time(end)
+    start.record(stream)
+    cp = pop.coupling_products(v, x0)
+    end.record(stream)
+    torch.cuda.synchronize()
+    t_cp = start.elapsed_time(end)
+    # central differences of L(theta) = Re <v, H(theta) x>, h = 1e-6
+    h = 1e-6
+    fd = []
+    for i in range(3):
+        tp, tm = list(theta0), list(theta0)
+        tp[i] += h
+        tm[i] -= h
+        lp = float(torch.real(torch.vdot(v, pop.apply(torch.tensor(tp, dtype=torch.float64), x0))))
+        lm = float(torch.real(torch.vdot(v, pop.apply(torch.tensor(tm, dtype=torch.float64), x0))))
+        fd.append((lp - lm) / (2 * h))
+    g = gtheta.numpy().tolist()
+    line = {
+        "metric": "H*x matrix elements/s", "value": value, "unit": "elements/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": args.config, "description": c["description"], "number_states": D, "nnz": nnz,
+                   "rhs": 1, "parallelism": "replicas", "l2": "inputs larger than L2 (x, v 16 B/state)"},
+        "cpu_baseline": None, "gpu_launches": None, "clocks": clocks.summary(), "basis_build_s": t_build,
+        "extra": {"forward_ms": t_fwd, "adjoint_ms": t_adj, "coupling_products_ms": t_cp,
+                  "grad_theta": g, "grad_theta_central_fd": fd,
+                  "max_rel_diff_grad_vs_fd": max(abs(a - b) / max(1.0, abs(b)) for a, b in zip(g, fd)),
+                  "loss": loss.item()},
     }
     print(json.dumps(line))
     return 0
@@ -579,11 +676,15 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
-    if args.config in ("xxz24_sectors", "xxz28_sectors", "hubbard16"):
+    if args.config in ("xxz24_sectors", "xxz28_sectors", "hubbard16", "ladder28_grad"):
         world, rank, _ = dist_setup()
         if rank != 0:
             return 0  # single-GPU workloads: under torchrun only rank 0 runs them
-        return run_hubbard(args) if args.config == "hubbard16" else run_sectors(args)
+        if args.config == "hubbard16":
+            return run_hubbard(args)
+        if args.config == "ladder28_grad":
+            return run_ladder(args)
+        return run_sectors(args)
 
     import torch
 

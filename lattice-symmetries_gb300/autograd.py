@@ -117,6 +117,9 @@ class ParametrizedOperator:
 
         if not isinstance(theta, torch.Tensor):
             theta = torch.as_tensor(theta, dtype=torch.float64)
+        if theta.dtype != torch.float64:
+            raise TypeError("theta must be float64 (got {}): the couplings are used in double precision".format(
+                theta.dtype))
         return _HApply.apply(theta, x, self)
 
 

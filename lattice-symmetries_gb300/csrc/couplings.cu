@@ -16,7 +16,7 @@ extern const uint64_t* device_binomials();
 constexpr int kMaxCouplings = 4;
 
 template <int GPL, bool INV>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
     k_coupling_products(const MatvecProblem p, const PackedLayout L, size_t off_cpl, int nc,
                         const double* __restrict__ g, const double* __restrict__ x,
                         double2* __restrict__ partial, int* __restrict__ err,
@@ -124,12 +124,22 @@ __global__ void __launch_bounds__(256)
         double2 c = T.tv[t];
         if (__popcll(beta & T.ts[t]) & 1) c = make_double2(-c.x, -c.y);
         uint64_t cand[GPL];
+        if (((info >> 16) & 0xffu) == 2u) {  // two flipped sites: their images directly
+          const uint64_t* r0 = ohl + (int)(info & 0xffu) * Gp;
+          const uint64_t* r1 = ohl + (int)((info >> 8) & 0xffu) * Gp;
 #pragma unroll
-        for (int k = 0; k < GPL; ++k) {
-          uint64_t v = ga[k];
-          for (uint64_t bits = xt; bits != 0; bits &= bits - 1)
-            v ^= ohl[(__ffsll((long long)bits) - 1) * Gp + 32 * k];
-          cand[k] = INV ? flip_packed(v, flipkey) : v;
+          for (int k = 0; k < GPL; ++k) {
+            cand[k] = ga[k] ^ r0[32 * k] ^ r1[32 * k];
+            if (INV) cand[k] = flip_packed(cand[k], flipkey);
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < GPL; ++k) {
+            uint64_t v = ga[k];
+            for (uint64_t bits = xt; bits != 0; bits &= bits - 1)
+              v ^= ohl[(__ffsll((long long)bits) - 1) * Gp + 32 * k];
+            cand[k] = INV ? flip_packed(v, flipkey) : v;
+          }
         }
 #pragma unroll
         for (int w2 = 1; w2 < GPL; w2 *= 2) {

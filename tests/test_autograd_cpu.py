@@ -53,3 +53,12 @@ def test_tagged_terms_equal_merged_expression(theta):
     y1 = ref.oracle_matvec(states, x, complex_=True)
     y2 = tagged.oracle_matvec(states, x, complex_=True)
     assert np.linalg.norm(y1 - y2) <= 1e-13 * np.linalg.norm(y1)
+
+
+def test_theta_must_be_double_precision():
+    torch = pytest.importorskip("torch")
+    n = 4
+    basis = ls.SpinBasis(2 * n, n, None, ls.Symmetries(LAT.ladder_symmetries(n, 0, 0)))
+    pop = ag.ParametrizedOperator(basis, ladder_parts(n))
+    with pytest.raises(TypeError):
+        pop.apply(torch.tensor([1.0, 0.7, 0.2]), None)  # float32: 1e-6 steps would be lost to rounding
