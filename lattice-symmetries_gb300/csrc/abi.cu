@@ -1058,25 +1058,28 @@ OperatorCache* operator_cache(const ls_hs_operator* op) {
 int ensure_norms(IndexData* ix, const OrbitData* od) {
   if (ix->d_norms != nullptr && ix->norms_for == od) return 0;
   cudaStream_t s = default_stream();
+  // one allocation: norms [n] | inverse norms [n]
+  const int64_t n = std::max<int64_t>(ix->n_states, 1);
   if (ix->d_norms == nullptr &&
-      !cuda_ok(cudaMalloc((void**)&ix->d_norms, std::max<int64_t>(ix->n_states, 1) * 8), "cudaMalloc(norms)"))
+      !cuda_ok(cudaMalloc((void**)&ix->d_norms, (size_t)n * 2 * 8), "cudaMalloc(norms)"))
     return LS_GPU_ERR_CUDA;
   int rc;
   if (od != nullptr && od->n_elems > 0) {
     const DeviceGroup* dg = orbit_device(od);
     rc = dg ? launch_orbit_norms(*dg, ix->n_states, ix->d_reps, ix->d_norms, s) : LS_GPU_ERR_CUDA;
-    // The norms are computed on the library's stream but read by kernels on the caller's stream:
-    // finish them before any caller can launch.
-    if (rc == 0) rc = cuda_ok(cudaStreamSynchronize(s), "orbit norms") ? 0 : LS_GPU_ERR_CUDA;
   } else {
-    std::vector<double> ones((size_t)std::max<int64_t>(ix->n_states, 1), 1.0);
+    std::vector<double> ones((size_t)n, 1.0);
     rc = cuda_ok(cudaMemcpyAsync(ix->d_norms, ones.data(), ones.size() * 8, cudaMemcpyHostToDevice, s),
                  "norms") ? 0 : LS_GPU_ERR_CUDA;
-    if (rc == 0) rc = cuda_ok(cudaStreamSynchronize(s), "norms") ? 0 : LS_GPU_ERR_CUDA;
   }
+  if (rc == 0) rc = launch_inverse_norms(ix->d_norms, ix->n_states, ix->d_norms + n, s);
+  // The norms are computed on the library's stream but read by kernels on the caller's stream:
+  // finish them before any caller can launch.
+  if (rc == 0) rc = cuda_ok(cudaStreamSynchronize(s), "orbit norms") ? 0 : LS_GPU_ERR_CUDA;
   if (rc == 0) {
     ix->norms_for = od;
     ix->dev.norms = ix->d_norms;
+    ix->dev.inv_norms = ix->d_norms + n;
   }
   return rc;
 }

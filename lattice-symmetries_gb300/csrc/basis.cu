@@ -401,6 +401,19 @@ static DeviceGroup strip(const DeviceGroup& g) {
   return h;
 }
 
+__global__ void k_inverse_norms(const double* __restrict__ norms, int64_t n, double* __restrict__ inv) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = norms[i];
+    inv[i] = v == 0.0 ? 0.0 : 1.0 / v;
+  }
+}
+
+int launch_inverse_norms(const double* d_norms, int64_t n, double* d_inv, cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_inverse_norms<<<grid_for(n, 256), 256, 0, s>>>(d_norms, n, d_inv);
+  return cuda_ok(cudaGetLastError(), "k_inverse_norms") ? 0 : LS_GPU_ERR_CUDA;
+}
+
 int launch_state_info(const DeviceGroup& g0, int64_t n, const uint64_t* d_x, uint64_t* d_rep,
                       double2* d_char, double* d_norm, int lane_width, cudaStream_t s) {
   (void)lane_width;  // encoded in g.prio

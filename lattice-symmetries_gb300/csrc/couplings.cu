@@ -56,12 +56,12 @@ __global__ void __launch_bounds__(256, 2)
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t row = warp_id; row < p.n_rows; row += n_warps) {
     const uint64_t a = __ldg(ix.reps + row);
-    const double na = __ldg(ix.norms + row);
-    if (na == 0.0) continue;  // zero-norm representative: zero row
+    const double inv_na = __ldg(ix.inv_norms + row);
+    if (inv_na == 0.0) continue;  // zero-norm representative: zero row
     const double2 gi = __ldg(Gv + row);
     const double2 xi = __ldg(X + row);
     const C2 gx = cmul_conj_b(C2{xi.x, xi.y}, C2{gi.x, gi.y});  // conj(g_i) x_i
-    const C2 w{gi.x / na, -gi.y / na};                           // conj(g_i) / n_i
+    const C2 w{gi.x * inv_na, -gi.y * inv_na};                   // conj(g_i) / n_i
 
     for (int t = lane; t < T.nd; t += 32) {
       if ((a & T.dm[t]) == T.dr[t]) {

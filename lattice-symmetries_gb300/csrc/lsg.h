@@ -73,6 +73,7 @@ struct DeviceIndex {
   int64_t n_states = 0;
   const uint64_t* reps = nullptr;
   const double* norms = nullptr;      // state_info norms of the representatives
+  const double* inv_norms = nullptr;  // 1 / norm (0 for a zero norm): no division per row
   const int64_t* offsets = nullptr;   // [2^prefix_bits] window starts (clamped), or null
   int shift = 0;                      // bucket = state >> shift
   int64_t range_size = 0;             // window length
@@ -162,6 +163,8 @@ int launch_is_representative(const DeviceGroup& g, int64_t n, const uint64_t* d_
                              uint8_t* d_flag, double* d_norm, int lane_width, cudaStream_t s);
 int launch_orbit_norms(const DeviceGroup& g, int64_t n, const uint64_t* d_reps, double* d_norms,
                        cudaStream_t s);
+// inv[i] = 1 / norms[i], or 0 where norms[i] == 0.
+int launch_inverse_norms(const double* d_norms, int64_t n, double* d_inv, cudaStream_t s);
 int compute_site_images(OrbitData* od);          // host tables (no GPU needed)
 const DeviceGroup* orbit_device(const OrbitData* od);  // uploads on first use; null on failure
 

@@ -205,8 +205,8 @@ __global__ void __launch_bounds__(256, 2)
 
   for (int64_t row = warp_id; row < p.n_rows; row += n_warps) {
     const uint64_t a = __ldg(p.index.reps + row);
-    const double na = __ldg(p.index.norms + row);
-    if (na == 0.0) {  // zero-norm representative: zero row and column (see packed_row)
+    const double inv_na = __ldg(p.index.inv_norms + row);
+    if (inv_na == 0.0) {  // zero-norm representative: zero row and column (see packed_row)
       if (lane < K) {
         if constexpr (CPLX) reinterpret_cast<double2*>(y)[row * ldy + lane] = make_double2(0.0, 0.0);
         else y[row * ldy + lane] = 0.0;
@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(256, 2)
         if (j >= 0) {
           double2 chi = S.chars[my_idx >> 1];
           if (INV && (my_idx & 1) && p.group.spin_inversion == -1) chi = make_double2(-chi.x, -chi.y);
-          const double ratio = nj / na;
+          const double ratio = nj * inv_na;
           const C2 f = cmul_conj_b(C2{my_c.x, my_c.y}, C2{chi.x, chi.y});
           fre = f.re * ratio;
           fim = f.im * ratio;
@@ -499,11 +499,11 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
   const int nt = T.nt;
 
   const uint64_t a = __ldg(ix.reps + row);
-  const double na = __ldg(ix.norms + row);
-  if (na == 0.0) {
+  const double inv_na = __ldg(ix.inv_norms + row);
+  if (inv_na == 0.0) {
     // A representative whose orbit norm is zero spans no state of the sector (the reference's
     // floating stabiliser sum can keep such states as rounding residue in complex sectors): its
-    // row and column of H are zero.  `na` is the same on every lane, so the warp stays converged.
+    // row and column of H are zero.  The value is the same on every lane: the warp stays converged.
     if (lane < K) {
       if constexpr (CPLX) reinterpret_cast<double2*>(y)[row * ldy + lane] = make_double2(0.0, 0.0);
       else y[row * ldy + lane] = 0.0;
@@ -666,7 +666,6 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
     if (lane == 0 && total) atomicAdd(nnz_counter, (unsigned long long)total);
   }
 
-  const double inv_na = 1.0 / na;
   if constexpr (CPLX) {
 #pragma unroll
     for (int d = 16; d >= K; d >>= 1) {
