@@ -535,9 +535,11 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
 
   Acc acc;
   unsigned found = 0;
+  // Lane s of the warp owns the s-th generated element since the last flush: the winning key
+  // (representative + group slot) and the term that generated it.  The element's coefficient,
+  // its sign and the state beta are only needed by the owning lane, at the flush.
   uint64_t my_key = ~0ull;
-  uint64_t my_beta = 0;  // the generated state (fermionic groups: its sign under the winning element)
-  double2 my_c = make_double2(0.0, 0.0);
+  int my_t = 0;
   int nslot = 0;
 
   auto flush = [&]() {
@@ -551,14 +553,20 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
       if (nj == 0.0) j = -1;  // zero-norm column
       found += (j >= 0);
       if (j >= 0) {
+        const uint64_t beta = a ^ T.tx[my_t];
+        // coefficient v_t (-1)^popcount(beta & s_t), the sign applied to the sign bits
+        double2 c = T.tv[my_t];
+        const long long sbit = (long long)(__popcll(beta & T.ts[my_t]) & 1) << 63;
+        c.x = __longlong_as_double(__double_as_longlong(c.x) ^ sbit);
+        c.y = __longlong_as_double(__double_as_longlong(c.y) ^ sbit);
         double2 chi = chars[idx >> 1];
         if (INV && (idx & 1) && spin_inversion == -1) chi = make_double2(-chi.x, -chi.y);
         if constexpr (FERMI) {
           // g moves the fermions of beta onto the representative with the sign of the
           // permutation it induces on the occupied orbitals (one lane per element)
-          if (fermion_parity(T.fs + (idx >> 1), Gp, my_beta)) chi = make_double2(-chi.x, -chi.y);
+          if (fermion_parity(T.fs + (idx >> 1), Gp, beta)) chi = make_double2(-chi.x, -chi.y);
         }
-        const C2 f = cmul_conj_b(C2{my_c.x, my_c.y}, C2{chi.x, chi.y});
+        const C2 f = cmul_conj_b(C2{c.x, c.y}, C2{chi.x, chi.y});
         fre = f.re * nj;
         fim = f.im * nj;
       }
@@ -607,19 +615,11 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
       mask &= mask - 1;
       const uint64_t xt = T.tx[t];
       const uint32_t info = T.ti[t];
-      const uint64_t beta = a ^ xt;
       if (info & kTermNeedsCheck) {
-        if (!constraint_ok(cons, beta)) {
+        if (!constraint_ok(cons, a ^ xt)) {
           if (lane == 0) atomicOr(err, 1);
           continue;
         }
-      }
-      // coefficient sign (-1)^popcount(beta & s) applied to the sign bits (integer ops)
-      double2 c = T.tv[t];
-      {
-        const long long sbit = (long long)(__popcll(beta & T.ts[t]) & 1) << 63;
-        c.x = __longlong_as_double(__double_as_longlong(c.x) ^ sbit);
-        c.y = __longlong_as_double(__double_as_longlong(c.y) ^ sbit);
       }
       uint64_t cand[GPL];
       if (((info >> 16) & 0xffu) == 2u) {
@@ -651,8 +651,7 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
       const uint32_t mlo = __reduce_min_sync(FULL, hi == mhi ? lo : 0xffffffffu);
       if (lane == nslot) {
         my_key = ((uint64_t)mhi << 32) | mlo;
-        my_c = c;
-        if constexpr (FERMI) my_beta = beta;
+        my_t = t;
       }
       if (++nslot == 32) {
         flush();
