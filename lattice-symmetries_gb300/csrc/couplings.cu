@@ -83,9 +83,10 @@ __global__ void __launch_bounds__(256, 2)
 #pragma unroll
     for (int k = 0; k < GPL; ++k) ga[k] |= (uint64_t)(2 * (lane + 32 * k));
 
+    // the owning lane of each element keeps its key and term; coefficient, sign and coupling
+    // are read at the flush
     uint64_t my_key = ~0ull;
-    double2 my_c = make_double2(0.0, 0.0);
-    int my_cid = 0;
+    int my_t = 0;
     int nslot = 0;
     auto flush = [&]() {
       if (lane < nslot) {
@@ -94,6 +95,9 @@ __global__ void __launch_bounds__(256, 2)
         const int64_t j = mv_index_lookup(ix, rep, binom);
         const double nj = j >= 0 ? __ldg(ix.norms + j) : 0.0;
         if (nj != 0.0) {
+          double2 my_c = T.tv[my_t];
+          if (__popcll((a ^ T.tx[my_t]) & T.ts[my_t]) & 1) my_c = make_double2(-my_c.x, -my_c.y);
+          const int my_cid = cpl_off[my_t];
           double2 chi = T.ch[idx >> 1];
           if (INV && (idx & 1) && p.group.spin_inversion == -1) chi = make_double2(-chi.x, -chi.y);
           const C2 f = cmul_conj_b(C2{my_c.x * nj, my_c.y * nj}, C2{chi.x, chi.y});
@@ -114,15 +118,12 @@ __global__ void __launch_bounds__(256, 2)
         mask &= mask - 1;
         const uint64_t xt = T.tx[t];
         const uint32_t info = T.ti[t];
-        const uint64_t beta = a ^ xt;
         if (info & kTermNeedsCheck) {
-          if (!constraint_ok(p.constraint, beta)) {
+          if (!constraint_ok(p.constraint, a ^ xt)) {
             if (lane == 0) atomicOr(err, 1);
             continue;
           }
         }
-        double2 c = T.tv[t];
-        if (__popcll(beta & T.ts[t]) & 1) c = make_double2(-c.x, -c.y);
         uint64_t cand[GPL];
         if (((info >> 16) & 0xffu) == 2u) {  // two flipped sites: their images directly
           const uint64_t* r0 = ohl + (int)(info & 0xffu) * Gp;
@@ -151,8 +152,7 @@ __global__ void __launch_bounds__(256, 2)
         const uint32_t mlo = __reduce_min_sync(FULL, hi == mhi ? lo : 0xffffffffu);
         if (lane == nslot) {
           my_key = ((uint64_t)mhi << 32) | mlo;
-          my_c = c;
-          my_cid = cpl_off[t];
+          my_t = t;
         }
         if (++nslot == 32) {
           flush();

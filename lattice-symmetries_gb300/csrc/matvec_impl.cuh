@@ -510,13 +510,24 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
     }
     return;
   }
+  // g.a for this lane's slots: XOR of the one-hot images of a's set bits, two bits at a time
+  // (one three-input XOR per pair)
   uint64_t ga[GPL];
 #pragma unroll
   for (int k = 0; k < GPL; ++k) ga[k] = 0;
-  for (uint64_t bits = a; bits != 0; bits &= bits - 1) {
-    const uint64_t* r = ohl + (__ffsll((long long)bits) - 1) * Gp;
+  uint64_t bits = a;
+  while (bits != 0) {
+    const uint64_t* r0 = ohl + (__ffsll((long long)bits) - 1) * Gp;
+    bits &= bits - 1;
+    if (bits == 0) {
 #pragma unroll
-    for (int k = 0; k < GPL; ++k) ga[k] ^= r[32 * k];
+      for (int k = 0; k < GPL; ++k) ga[k] ^= r0[32 * k];
+      break;
+    }
+    const uint64_t* r1 = ohl + (__ffsll((long long)bits) - 1) * Gp;
+    bits &= bits - 1;
+#pragma unroll
+    for (int k = 0; k < GPL; ++k) ga[k] ^= r0[32 * k] ^ r1[32 * k];
   }
 #pragma unroll
   for (int k = 0; k < GPL; ++k) ga[k] |= (uint64_t)(2 * (lane + 32 * k));
