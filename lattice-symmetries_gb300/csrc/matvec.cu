@@ -56,6 +56,18 @@ void get_matvec_config(int* threads, int* waves, int* rhs_tile) {
 
 extern const uint64_t* device_binomials();
 
+// xs[i][c] = x[i][c] * norms[i] for k columns of `words` doubles per element (1 real, 2 complex).
+__global__ void k_prescale(const double* __restrict__ x, int64_t ldx, const double* __restrict__ norms, int64_t n,
+                           int k, int words, double* __restrict__ xs) {
+  const int64_t per_row = (int64_t)k * words;
+  const int64_t total = n * per_row;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / per_row, r = e - i * per_row;
+    xs[e] = __ldg(x + i * ldx * words + r) * __ldg(norms + i);
+  }
+}
+
+
 constexpr size_t kMaxDynamicSmem = 200 * 1024;
 
 LaunchShape packed_shape(int64_t n_rows) {
@@ -83,8 +95,26 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
     const PackedLayout PL = make_packed_layout(p);
     const bool packed = p.group.gpl > 0 && p.group.onehot_packed != nullptr && PL.total <= kMaxDynamicSmem;
     if (packed) {
-      int done = 0;
-      while (done < k) {
+      // Gather source x_j * n_j for all k columns (one streaming pass), so that the kernels read
+      // no norm per generated element.  Not when counting elements (the count needs the norms).
+      MatvecProblem q = p;
+      double* d_xs = nullptr;
+      const size_t xs_bytes = (size_t)p.n_rows * k * scalar_words * sizeof(double);
+      if (p.nnz_counter == nullptr && p.index.norms != nullptr &&
+          cudaMallocAsync((void**)&d_xs, xs_bytes, s) == cudaSuccess) {
+        const int64_t total = p.n_rows * k * (int64_t)scalar_words;
+        const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 16));
+        k_prescale<<<blocks, 256, 0, s>>>(d_x, ldx, p.index.norms, p.n_rows, k, (int)scalar_words, d_xs);
+        if (!cuda_ok(cudaGetLastError(), "k_prescale")) {
+          cudaFreeAsync(d_xs, s);
+          return LS_GPU_ERR_CUDA;
+        }
+      } else {
+        cudaGetLastError();  // a failed stream-ordered allocation: gather x and the norms instead
+        d_xs = nullptr;
+      }
+      int done = 0, rc = 0;
+      while (done < k && rc == 0) {
         const int left = k - done;
         const int most = std::min(left, g_rhs_tile);
         int chunk = most >= 16 ? 16 : most >= 8 ? 8 : most >= 4 ? 4 : 1;
@@ -92,11 +122,13 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
         if (p.group.fermionic && !cplx) chunk = 1;  // fermionic real path: one column per launch
         const double* xs = d_x + (size_t)done * scalar_words;
         double* ys = d_y + (size_t)done * scalar_words;
-        int rc = launch_packed(cplx, chunk, p.group.gpl, inv, p, PL, sh, xs, ldx, ys, ldy, d_err, binom, s);
-        if (rc != 0) return rc;
+        q.xs = d_xs ? d_xs + (size_t)done * scalar_words : nullptr;
+        q.ldxs = k;
+        rc = launch_packed(cplx, chunk, p.group.gpl, inv, q, PL, sh, xs, ldx, ys, ldy, d_err, binom, s);
         done += chunk;
       }
-      return 0;
+      if (d_xs) cudaFreeAsync(d_xs, s);
+      return rc;
     }
     if (p.group.fermionic)
       return fail(LS_GPU_ERR_INVALID, "fermionic lattice symmetries need the packed kernel (tables too large)");

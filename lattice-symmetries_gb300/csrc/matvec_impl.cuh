@@ -485,7 +485,12 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
                                            const int64_t ldx, double* __restrict__ y, const int64_t ldy,
                                            const int64_t row, int* __restrict__ err,
                                            const uint64_t* __restrict__ binom,
-                                           unsigned long long* nnz_counter, const bool real_elements) {
+                                           unsigned long long* nnz_counter, const bool real_elements,
+                                           const double* __restrict__ xs = nullptr, const int64_t ldxs = 0) {
+  // gather source: x_j * n_j when prescaled (xs), else x_j with the norm applied per element
+  const bool prescaled = xs != nullptr;
+  const double* __restrict__ xg = prescaled ? xs : x;
+  const int64_t ldg = prescaled ? ldxs : ldx;
   constexpr unsigned FULL = 0xffffffffu;
   constexpr int Gp = 32 * GPL;
   constexpr int Q = 32 / K;
@@ -560,8 +565,9 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
       const uint64_t rep = my_key >> SH;
       const uint32_t idx = (uint32_t)(my_key & lowmask);
       j = mv_index_lookup(ix, rep, binom);
-      const double nj = j >= 0 ? __ldg(ix.norms + j) : 0.0;
-      if (nj == 0.0) j = -1;  // zero-norm column
+      // a zero-norm column contributes nothing (prescaled: its x_j * n_j is already zero)
+      const double nj = prescaled ? 1.0 : (j >= 0 ? __ldg(ix.norms + j) : 0.0);
+      if (nj == 0.0) j = -1;
       found += (j >= 0);
       if (j >= 0) {
         const uint64_t beta = a ^ T.tx[my_t];
@@ -578,8 +584,8 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
           if (fermion_parity(T.fs + (idx >> 1), Gp, beta)) chi = make_double2(-chi.x, -chi.y);
         }
         const C2 f = cmul_conj_b(C2{c.x, c.y}, C2{chi.x, chi.y});
-        fre = f.re * nj;
-        fim = f.im * nj;
+        fre = prescaled ? f.re : f.re * nj;
+        fim = prescaled ? f.im : f.im * nj;
       }
     }
     if (CPLX && real_elements) {
@@ -590,7 +596,7 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
         const int64_t js = (K == 1) ? j : __shfl_sync(FULL, j, src);
         const double sre = (K == 1) ? fre : __shfl_sync(FULL, fre, src);
         if (s < nslot && js >= 0) {
-          const double2 xv = __ldg(reinterpret_cast<const double2*>(x) + js * ldx + rhs);
+          const double2 xv = __ldg(reinterpret_cast<const double2*>(xg) + js * ldg + rhs);
           acc.re += sre * xv.x;
           acc.im += sre * xv.y;
         }
@@ -606,11 +612,11 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
       const double sim = (K == 1) ? fim : __shfl_sync(FULL, fim, src);
       if (s < nslot && js >= 0) {
         if constexpr (CPLX) {
-          const double2 xv = __ldg(reinterpret_cast<const double2*>(x) + js * ldx + rhs);
+          const double2 xv = __ldg(reinterpret_cast<const double2*>(xg) + js * ldg + rhs);
           acc.re += sre * xv.x - sim * xv.y;
           acc.im += sre * xv.y + sim * xv.x;
         } else {
-          acc.re += sre * __ldg(x + js * ldx + rhs);
+          acc.re += sre * __ldg(xg + js * ldg + rhs);
         }
       }
       if (K == 1) break;
@@ -708,7 +714,8 @@ __global__ void __launch_bounds__(320, 2)
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t row = warp_id; row < p.n_rows; row += n_warps)
     packed_row<GPL, INV, CPLX, K, FERMI>(T, p.group.n_bits, p.index, T.ch, p.group.spin_inversion, p.constraint, x, ldx,
-                                  y, ldy, row, err, binom, p.nnz_counter, p.real_elements != 0);
+                                  y, ldy, row, err, binom, p.nnz_counter, p.real_elements != 0,
+                                  p.xs, p.ldxs);
 }
 
 // Batched kernel: the rows of all sectors form one row space that a persistent grid walks; each
