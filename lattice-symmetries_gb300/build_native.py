@@ -81,7 +81,8 @@ def build(force: bool = False, verbose_ptxas: bool = False, jobs: int = 0) -> st
         with concurrent.futures.ThreadPoolExecutor(max_workers=jobs) as ex:
             for f in [ex.submit(_compile, s, verbose_ptxas) for s in todo]:
                 f.result()
-    if todo or not os.path.exists(LIB_PATH):
+    # relink when an object is newer than the library (also after a link that failed)
+    if todo or not os.path.exists(LIB_PATH) or _stale(LIB_PATH, objs):
         tmp = LIB_PATH + ".tmp"
         cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "shared", "-o", tmp] + objs
         res = subprocess.run(cmd, capture_output=True, text=True)
