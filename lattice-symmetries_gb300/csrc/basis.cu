@@ -1006,11 +1006,11 @@ int enumerate_states(const DeviceGroup* g0, const EnumerateRequest& req, uint64_
 // Prefix-bucket index (indexing.c:45-117 semantics, built on the device)
 // ------------------------------------------------------------------------------------------------
 __global__ void k_bucket_offsets(const uint64_t* __restrict__ reps, int64_t n, int shift,
-                                 int64_t n_buckets, int64_t* __restrict__ offsets) {
+                                 int64_t n_buckets, uint32_t* __restrict__ offsets) {
   for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b <= n_buckets;
        b += (int64_t)gridDim.x * blockDim.x) {
     if (b == n_buckets) {
-      offsets[b] = n;
+      offsets[b] = (uint32_t)n;
       continue;
     }
     // first k with (reps[k] >> shift) >= b
@@ -1019,11 +1019,11 @@ __global__ void k_bucket_offsets(const uint64_t* __restrict__ reps, int64_t n, i
       const int64_t mid = (lo + hi) >> 1;
       if ((reps[mid] >> shift) < (uint64_t)b) lo = mid + 1; else hi = mid;
     }
-    offsets[b] = lo;
+    offsets[b] = (uint32_t)lo;
   }
 }
 
-__global__ void k_bucket_max(const int64_t* __restrict__ offsets, int64_t n_buckets,
+__global__ void k_bucket_max(const uint32_t* __restrict__ offsets, int64_t n_buckets,
                              unsigned long long* __restrict__ out) {
   unsigned long long m = 0;
   for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < n_buckets;
@@ -1038,20 +1038,23 @@ __global__ void k_bucket_max(const int64_t* __restrict__ offsets, int64_t n_buck
   if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
-__global__ void k_bucket_clamp(int64_t* __restrict__ offsets, int64_t n_buckets, int64_t limit) {
+__global__ void k_bucket_clamp(uint32_t* __restrict__ offsets, int64_t n_buckets, int64_t limit) {
   for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < n_buckets;
        b += (int64_t)gridDim.x * blockDim.x) {
-    if (offsets[b] > limit) offsets[b] = limit;
+    if ((int64_t)offsets[b] > limit) offsets[b] = (uint32_t)limit;
   }
 }
 
 // The reference buckets on the top prefix_bits of number_bits (indexing.c:94-117).  Sorted
 // representatives are orbit minima and crowd towards small values, so here the buckets cover the
 // bits actually used (up to the largest representative) and their count grows with the basis
-// (about two states per bucket, at most 2^26 buckets); the answers are the same indices.
+// (about one state per bucket) up to 2^24 buckets of 32-bit starts (a 64 MB table, most of which
+// stays in L2 while the matvec probes it once per generated element).  The answers are the same
+// indices.
 int build_prefix_index(const uint64_t* d_reps, int64_t n, int number_bits, int prefix_bits,
-                       int64_t** d_offsets, int64_t* range_size, int* shift, cudaStream_t s,
+                       uint32_t** d_offsets, int64_t* range_size, int* shift, cudaStream_t s,
                        uint64_t* max_state) {
+  if (n >= ((int64_t)1 << 32)) return fail(LS_GPU_ERR_INVALID, "more than 2^32 representatives");
   uint64_t max_rep = 0;
   if (n > 0 && !cuda_ok(cudaMemcpyAsync(&max_rep, d_reps + (n - 1), 8, cudaMemcpyDeviceToHost, s), "read max") )
     return LS_GPU_ERR_CUDA;
@@ -1059,15 +1062,15 @@ int build_prefix_index(const uint64_t* d_reps, int64_t n, int number_bits, int p
   *max_state = n > 0 ? max_rep : 0;
   const int used_bits = max_rep == 0 ? 1 : 64 - __builtin_clzll(max_rep);
   int want = 1;
-  while (want < 26 && ((int64_t)1 << want) < n) ++want;
+  while (want < 24 && ((int64_t)1 << want) < n) ++want;
   int p = std::max(std::min(prefix_bits, number_bits), want);
-  p = std::min(p, std::min(used_bits, 26));
+  p = std::min(p, std::min(used_bits, 24));
   if (p < 0) p = 0;
   *shift = used_bits - p;
   const int64_t nb = (int64_t)1 << p;
-  int64_t* off = nullptr;
+  uint32_t* off = nullptr;
   unsigned long long* mx = nullptr;
-  if (!cuda_ok(cudaMalloc((void**)&off, (nb + 1) * 8), "alloc offsets") ||
+  if (!cuda_ok(cudaMalloc((void**)&off, (nb + 1) * 4), "alloc offsets") ||
       !cuda_ok(cudaMalloc((void**)&mx, 8), "alloc")) {
     cudaFree(off);
     return LS_GPU_ERR_CUDA;

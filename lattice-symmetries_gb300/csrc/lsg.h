@@ -74,7 +74,7 @@ struct DeviceIndex {
   const uint64_t* reps = nullptr;
   const double* norms = nullptr;      // state_info norms of the representatives
   const double* inv_norms = nullptr;  // 1 / norm (0 for a zero norm): no division per row
-  const int64_t* offsets = nullptr;   // [2^prefix_bits] window starts (clamped), or null
+  const uint32_t* offsets = nullptr;  // [2^prefix_bits + 1] window starts (clamped), or null
   int shift = 0;                      // bucket = state >> shift
   int64_t range_size = 0;             // window length
   int prefix_bits = 0;
@@ -138,7 +138,7 @@ struct IndexData {
   int prefix_bits;
   DeviceIndex dev;
   uint64_t* d_reps = nullptr;
-  int64_t* d_offsets = nullptr;
+  uint32_t* d_offsets = nullptr;
   double* d_norms = nullptr;          // filled lazily when a projected matvec needs them
   const OrbitData* norms_for = nullptr;
 };
@@ -189,7 +189,7 @@ int enumerate_states_noalloc(const OrbitData* od, const EnumerateRequest& req, u
 int exclusive_scan_counts(const int32_t* d_in, int64_t n, int64_t* d_out, cudaStream_t s);
 
 int build_prefix_index(const uint64_t* d_reps, int64_t n, int number_bits, int prefix_bits,
-                       int64_t** d_offsets, int64_t* range_size, int* shift, cudaStream_t s,
+                       uint32_t** d_offsets, int64_t* range_size, int* shift, cudaStream_t s,
                        uint64_t* max_state);
 int launch_state_index(const DeviceIndex& ix, int64_t n, const uint64_t* d_x, int64_t* d_out,
                        cudaStream_t s);
