@@ -37,7 +37,7 @@ if REPO not in sys.path:
 # DRAM bytes (read + write) of one matvec launch from an ncu capture of the same workload, with the
 # integer (ALU) pipe utilisation of that capture; summaries and commands in profiles/.
 NCU_CAPTURES = {
-    "j1j2_6x6": {"traffic": 117.884e9 + 0.272e9, "alu_pipe_pct": 66.9,
+    "j1j2_6x6": {"traffic": 117.870e9 + 0.269e9, "alu_pipe_pct": 73.4,
                  "source": "profiles/k_matvec_packed_j1j2_6x6.md"},
 }
 
