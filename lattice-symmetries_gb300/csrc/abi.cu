@@ -70,6 +70,15 @@ DeviceRuntime& rt() {
     }
     cudaMalloc((void**)&r.binom, sizeof(table));
     cudaMemcpy(r.binom, table, sizeof(table), cudaMemcpyHostToDevice);
+    // Stream-ordered allocations (the matvec's prescaled gather source, scan scratch) come from
+    // the device's default memory pool: keep freed blocks in this process's pool instead of
+    // returning them at every synchronisation, so that repeated matvecs (and graph replays) do
+    // not map memory again.  A process-local allocator attribute, not a device setting.
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     r.ready = true;
   }
   return r;
