@@ -392,8 +392,10 @@ int ls_gpu_state_index(ls_hs_basis const *basis, int64_t batch, uint64_t const *
 int ls_gpu_enumerate_noalloc(ls_hs_basis const *basis, uint64_t *d_out, int64_t capacity,
                              int64_t *count, void *stream);
 
-/* Tuning knobs of the projected matvec kernels: threads per CTA (256 or 320) and grid waves (the
- * grid is 2 * SMs * waves CTAs, one warp per row at a time); 0 = default (256, 4). */
+/* Tuning knobs of the projected matvec kernels: threads per CTA (a multiple of 32, at most 320)
+ * and grid waves (the grid is 2 * SMs * waves CTAs, one warp per row at a time); 0 = default
+ * (320, 8).  The fallback kernel for groups whose packed tables do not fit (or 64-bit states)
+ * always runs 256-thread CTAs. */
 int ls_gpu_set_matvec_config(int threads_per_block, int waves);
 /* Most right-hand sides per kernel launch (16, 8, 4 or 1; larger k is split into launches). */
 int ls_gpu_set_matvec_rhs_tile(int rhs_tile);

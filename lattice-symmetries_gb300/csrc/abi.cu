@@ -261,8 +261,9 @@ extern "C" int ls_gpu_get_matvec_config(int* threads_per_block, int* waves, int*
 }
 
 extern "C" int ls_gpu_set_matvec_config(int threads_per_block, int blocks_per_sm) {
-  if (threads_per_block != 0 && (threads_per_block % 32 != 0 || threads_per_block > 1024))
-    return fail(LS_GPU_ERR_INVALID, "threads_per_block must be a multiple of 32, at most 1024");
+  if (threads_per_block != 0 && (threads_per_block % 32 != 0 || threads_per_block > 320))
+    return fail(LS_GPU_ERR_INVALID, "threads_per_block must be a multiple of 32, at most 320");
+  if (blocks_per_sm < 0 || blocks_per_sm > 64) return fail(LS_GPU_ERR_INVALID, "waves must be in [0, 64]");
   return set_matvec_config(threads_per_block, blocks_per_sm);
 }
 

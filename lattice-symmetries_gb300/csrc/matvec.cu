@@ -37,6 +37,9 @@ static int g_blocks_per_sm_override = 0;
 static int g_rhs_tile = 16;  // most right-hand sides per launch (16, 8, 4 or 1)
 
 int set_matvec_config(int threads, int blocks_per_sm) {
+  // the warp-per-row kernels are compiled for at most 320 threads per block
+  if (threads != 0 && (threads < 32 || threads > 320 || threads % 32 != 0)) return LS_GPU_ERR_INVALID;
+  if (blocks_per_sm < 0 || blocks_per_sm > 64) return LS_GPU_ERR_INVALID;
   g_threads_override = threads;
   g_blocks_per_sm_override = blocks_per_sm;
   return 0;
@@ -136,11 +139,15 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
     if (gpl < 0) return fail(LS_GPU_ERR_INVALID, "symmetry group too large for the matvec kernels");
     const SmemLayout L = make_layout(p, true);
     if (L.total > kMaxDynamicSmem) return fail(LS_GPU_ERR_INVALID, "term tables too large for shared memory");
+    // the fallback kernel is compiled for at most 256 threads per block
+    const LaunchShape shf{(int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sh.blocks * sh.threads / 256,
+                                                                      (p.n_rows + 7) / 8)),
+                          256};
     for (int c = 0; c < k; ++c) {
       const double* xs = d_x + (size_t)c * scalar_words;
       double* ys = d_y + (size_t)c * scalar_words;
-      int rc = cplx ? launch_projected_cplx_k1(gpl, inv, p, L, sh, xs, ldx, ys, ldy, d_err, binom, s)
-                    : launch_projected_real(gpl, inv, p, L, sh, xs, ldx, ys, ldy, d_err, binom, s);
+      int rc = cplx ? launch_projected_cplx_k1(gpl, inv, p, L, shf, xs, ldx, ys, ldy, d_err, binom, s)
+                    : launch_projected_real(gpl, inv, p, L, shf, xs, ldx, ys, ldy, d_err, binom, s);
       if (rc != 0) return rc;
     }
     return 0;
