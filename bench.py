@@ -58,7 +58,7 @@ CONFIGS = {
     "xxz24_sectors": dict(n=24, delta=1.5, rhs=16, lanczos_steps=100, seed=3,
                           description="XXZ chain N=24 PBC, Delta=1.5, Sz=0, 24 momenta x z=+-1 (48 sectors), "
                                       "16 RHS: the batched workload at a size for kernel profiles"),
-    "xxz28_sectors": dict(n=28, delta=1.5, rhs=16, lanczos_steps=100, seed=3,
+    "xxz28_sectors": dict(n=28, delta=1.5, rhs=16, lanczos_steps=100, lanczos_compare_steps=30, seed=3,
                           description="XXZ chain N=28 PBC, Jxy=1, Delta=1.5, Sz=0, all 28 momenta x z=+-1 "
                                       "(56 sectors), 16 complex RHS per sector, one batched launch in a CUDA "
                                       "graph, 100 block-Lanczos steps"),
@@ -468,6 +468,13 @@ def run_hubbard(args):
         ep = float(lanczos.ground_state_energy(pop, tp, k=k, steps=c["lanczos_steps"], seed=c["seed"]))
         em = float(lanczos.ground_state_energy(pop, tm, k=k, steps=c["lanczos_steps"], seed=c["seed"]))
         fd.append((ep - em) / (2 * h))
+    # the same Lanczos run with torch FP64 GEMMs for the dense products
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0_fp64 = float(lanczos.ground_state_energy(pop, list(theta0), k=k, steps=c["lanczos_steps"], seed=c["seed"],
+                                                dense="fp64"))
+    torch.cuda.synchronize()
+    t_fp64 = time.perf_counter() - t0
 
     bytes_per_launch = D * (16 + 32 * k) + nnz * (16 + 16 * k)
     achieved = bytes_per_launch / (t_ms * 1e-3) / 1e9
@@ -487,7 +494,9 @@ def run_hubbard(args):
         "extra": {"plain_one_vector_ms": t_plain, "speedup_per_vector_vs_plain": t_plain * k / t_ms,
                   "ground_state": {"E0": e0.item(), "lanczos_steps": c["lanczos_steps"], "seconds": t_lanczos,
                                    "dE0_dtheta_hellmann_feynman": hf, "dE0_dtheta_central_fd": fd,
-                                   "fd_step": h, "theta": theta0}},
+                                   "fd_step": h, "theta": theta0,
+                                   "dense": "FP32-pair Gram / update kernels (ls_gpu_block_gram, ls_gpu_block_update)",
+                                   "E0_fp64_dense": e0_fp64, "seconds_fp64_dense": t_fp64}},
     }
     print(json.dumps(line))
     return 0
@@ -582,6 +591,17 @@ def run_sectors(args):
     timer_lean = {}  # one Cholesky-QR pass, no local re-orthogonalisation
     e0_lean = lanczos.sector_ground_states(batch, steps=c["lanczos_steps"], seed=c["seed"], graph=True,
                                            timer=timer_lean, lean=True)
+    # the same recurrence with torch FP64 GEMMs for the dense products (fewer steps on the large
+    # workload: FP64 GEMMs are slow on GB300)
+    cmp_steps = c.get("lanczos_compare_steps", c["lanczos_steps"])
+    timer_pc = timer
+    e0_pc = e0
+    if cmp_steps != c["lanczos_steps"]:
+        timer_pc = {}
+        e0_pc = lanczos.sector_ground_states(batch, steps=cmp_steps, seed=c["seed"], graph=True, timer=timer_pc)
+    timer_f = {}
+    e0_f = lanczos.sector_ground_states(batch, steps=cmp_steps, seed=c["seed"], graph=True, timer=timer_f,
+                                        dense="fp64")
 
     bytes_per_launch = sum(sizes) * (16 + 32 * k) + sum(nnzs) * (16 + 16 * k)
     achieved = bytes_per_launch / (t_ms * 1e-3) / 1e9
@@ -611,8 +631,13 @@ def run_sectors(args):
                   "lanczos": {"steps": c["lanczos_steps"], "ms_per_step": timer["ms"] / timer["steps"],
                               "ground_state_energy": float(np.min(e0)),
                               "sector_of_ground_state": int(np.argmin(e0)),
+                              "dense": "FP32-pair Gram / update kernels (ls_gpu_block_gram, ls_gpu_block_update)",
                               "lean_ms_per_step": timer_lean["ms"] / timer_lean["steps"],
-                              "lean_max_abs_diff_sector_e0": float(np.max(np.abs(e0_lean - e0)))}},
+                              "lean_max_abs_diff_sector_e0": float(np.max(np.abs(e0_lean - e0))),
+                              "fp64_dense": {"steps": cmp_steps, "ms_per_step": timer_f["ms"] / timer_f["steps"],
+                                             "paired_ms_per_step": timer_pc["ms"] / timer_pc["steps"],
+                                             "max_abs_diff_sector_e0_vs_paired":
+                                                 float(np.max(np.abs(e0_f - e0_pc)))}}},
     }
     print(json.dumps(line))
     return 0

@@ -406,6 +406,28 @@ int ls_gpu_get_matvec_config(int *threads_per_block, int *waves, int *rhs_tile);
 int ls_gpu_autotune_matvec(ls_hs_operator const *op, int k, int *best_threads, int *best_waves,
                            double *best_ms);
 
+/* Dense products of the block eigensolver on tall complex128 blocks: S sectors of D rows and
+ * 1 <= k <= 16 columns, stored [S][D][k] row-major (interleaved re, im), device pointers.
+ *   ls_gpu_block_gram:   G[s] = X[s]^H Y[s], G [S][k][k]; X == Y allowed.
+ *   ls_gpu_block_update: out[s] = beta W[s] + X1[s] M1[s] + X2[s] M2[s], M [S][k][k]; X2 and M2
+ *                        are NULL together; W may be NULL when beta == 0; out may alias W, X1
+ *                        or X2 (each row is read before it is written).
+ * The blocks stay FP64 in memory; the products are evaluated in FP32-pair arithmetic (each
+ * FP64 input split into two floats, error-free hi*hi products, two-sum accumulation: about
+ * 2^-46 relative per product, every entry within ~1e-14 of the sum of its terms' magnitudes)
+ * because GB300's FP64 pipe is a small fraction of its FP32 rate.  Range: products of two
+ * entries must stay below ~1e38 in magnitude (else inf), and lose low-order bits below ~1e-30
+ * (orthonormal and H-applied blocks are far inside).
+ * Stream-ordered: the Gram allocates its partial sums with cudaMallocAsync on `stream`, so both
+ * can be recorded in a CUDA graph.  No reference counterpart: the reference's eigensolvers are
+ * scipy's eigsh over the matvec (python/lattice_symmetries/__init__.py:751-752) and PRIMME
+ * (chapel/src/Diagonalize.chpl). */
+int ls_gpu_block_gram(int64_t S, int64_t D, int k, double const *d_x, double const *d_y, double *d_g,
+                      void *stream);
+int ls_gpu_block_update(int64_t S, int64_t D, int k, double beta, double const *d_w,
+                        double const *d_x1, double const *d_m1, double const *d_x2,
+                        double const *d_m2, double *d_out, void *stream);
+
 #if defined(__cplusplus)
 } /* extern "C" */
 #endif

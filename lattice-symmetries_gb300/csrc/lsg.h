@@ -248,4 +248,11 @@ int launch_transpose(const double* d_in, double* d_out, int64_t rows, int64_t co
 int launch_coupling_products(const MatvecProblem& p, int n_couplings, const double* d_g,
                              const double* d_x, double* d_out, int* d_err, cudaStream_t s);
 
+// Dense products of the block eigensolver in FP32-pair arithmetic (blockops.cu).
+int launch_block_gram(int64_t S, int64_t D, int k, const double* d_x, const double* d_y, double* d_g,
+                      cudaStream_t s);
+int launch_block_update(int64_t S, int64_t D, int k, double beta, const double* d_w, const double* d_x1,
+                        const double* d_m1, const double* d_x2, const double* d_m2, double* d_out,
+                        cudaStream_t s);
+
 }  // namespace lsg

@@ -16,6 +16,12 @@ Recurrence (per sector, blocks of k columns, Q_0 orthonormal, Q_{-1} = 0, B_{-1}
 and the eigenvalues of the block-tridiagonal T (diagonal blocks A_j, sub-diagonal blocks B_j)
 approximate the extremal eigenvalues of H.  There is no global re-orthogonalisation, so converged
 Ritz values can repeat ("ghosts"); the lowest ones are reliable.
+
+Dense products (`dense=`): "paired" (default on the GPU for k <= 16) runs the tall-skinny Gram
+matrices and block updates through the library's FP32-pair kernels (ls_gpu_block_gram /
+ls_gpu_block_update: FP64 storage, about 2^-44 relative error per product, several times the
+speed of FP64 GEMMs on GB300, whose FP64 pipe is narrow); "fp64" uses torch's FP64 GEMMs.
+CPU tensors always take the torch path.
 """
 
 from __future__ import annotations
@@ -25,12 +31,42 @@ from typing import Callable, List, Optional, Tuple
 import numpy as np
 
 
-def _gram(X, Y, blocks: int = 256, min_rows: int = 64):
-    """X^H Y for [S, D, k] blocks as [S, k, k].  A single GEMM with inner dimension D (hundreds of
-    thousands) and a 16 x 16 output leaves most of the GPU idle, so the rows are split into
-    `blocks` equal row blocks (S * blocks GEMMs whose partial results are summed) plus the
+DENSE_DEFAULT = "paired"
+
+
+def _paired(X, dense) -> bool:
+    import torch
+
+    mode = DENSE_DEFAULT if dense is None else dense
+    if mode not in ("paired", "fp64"):
+        raise ValueError("dense must be 'paired' or 'fp64'")
+    return mode == "paired" and X.is_cuda and X.dtype == torch.complex128 and X.dim() == 3 and X.shape[-1] <= 16
+
+
+def _native():
+    from . import _native as N
+
+    return N, N.lib()
+
+
+def _gram(X, Y, dense=None, blocks: int = 256, min_rows: int = 64):
+    """X^H Y for [S, D, k] blocks as [S, k, k].
+
+    paired: one call of ls_gpu_block_gram.  fp64 (torch): a single GEMM with inner dimension D
+    (hundreds of thousands) and a 16 x 16 output leaves most of the GPU idle, so the rows are split
+    into `blocks` equal row blocks (S * blocks GEMMs whose partial results are summed) plus the
     remaining D mod blocks rows."""
+    import torch
+
     S, D, k = X.shape
+    if _paired(X, dense):
+        N, lib = _native()
+        X = X.contiguous()
+        Y = Y.contiguous()
+        G = torch.empty((S, k, k), dtype=X.dtype, device=X.device)
+        stream = torch.cuda.current_stream(X.device).cuda_stream
+        N.check(lib.ls_gpu_block_gram(S, D, k, X.data_ptr(), Y.data_ptr(), G.data_ptr(), stream), "block Gram")
+        return G
     c = blocks
     while c > 1 and D // c < min_rows:
         c //= 2
@@ -43,49 +79,90 @@ def _gram(X, Y, blocks: int = 256, min_rows: int = 64):
     return main + X[:, c * m:].mH @ Y[:, c * m:]
 
 
-def _cholqr(W, eps: float = 1e-15, passes: int = 2):
+def _update(out, beta: float, W, X1, M1, X2=None, M2=None, dense=None):
+    """out = beta W + X1 M1 (+ X2 M2) for [S, D, k] blocks and [S, k, k] matrices; out may be W, X1
+    or X2 (paired: one call of ls_gpu_block_update; fp64: torch GEMMs)."""
+    import torch
+
+    S, D, k = X1.shape
+    if _paired(X1, dense) and out.is_contiguous():
+        N, lib = _native()
+        X1 = X1.contiguous()
+        M1 = M1.contiguous()
+        if X2 is not None:
+            X2 = X2.contiguous()
+            M2 = M2.contiguous()
+        if W is not None and beta != 0.0:
+            W = W.contiguous()
+        stream = torch.cuda.current_stream(X1.device).cuda_stream
+        rc = lib.ls_gpu_block_update(S, D, k, float(beta), W.data_ptr() if (W is not None and beta != 0.0) else None,
+                                     X1.data_ptr(), M1.data_ptr(), X2.data_ptr() if X2 is not None else None,
+                                     M2.data_ptr() if M2 is not None else None, out.data_ptr(), stream)
+        N.check(rc, "block update")
+        return out
+    if beta != 0.0 and out is W and X1 is not out and X2 is not out:
+        if beta != 1.0:
+            out.mul_(beta)
+        out.baddbmm_(X1, M1)
+        if X2 is not None:
+            out.baddbmm_(X2, M2)
+        return out
+    res = torch.matmul(X1, M1)
+    if X2 is not None:
+        res = res + torch.matmul(X2, M2)
+    if beta != 0.0:
+        res = res + beta * W
+    out.copy_(res)
+    return out
+
+
+def _cholqr(W, eps: float = 1e-15, passes: int = 2, dense=None, out=None):
     """W = Q R with Q orthonormal (batched over the leading dimension): two Cholesky-QR passes.
     A tiny diagonal shift keeps exhausted blocks (W ~ 0) finite instead of NaN.  The k x k factor
-    is inverted explicitly, so that applying it is a GEMM rather than a triangular solve over D."""
+    is inverted explicitly, so that applying it is a GEMM rather than a triangular solve over D.
+    With `out`, Q is written there and W serves as scratch for the intermediate passes."""
     import torch
 
     k = W.shape[-1]
     eye = torch.eye(k, dtype=W.dtype, device=W.device)
     R = None
     Q = W
-    for _ in range(passes):
-        G = _gram(Q, Q)
+    for p in range(passes):
+        G = _gram(Q, Q, dense)
         G = 0.5 * (G + G.mH)
         scale = torch.diagonal(G, dim1=-2, dim2=-1).real.mean(-1).clamp_min(1e-300)
         G = G + (eps * scale)[..., None, None] * eye
         L, _ = torch.linalg.cholesky_ex(G)
         Rp = L.mH
         Rinv = torch.linalg.solve_triangular(Rp, eye.expand_as(Rp), upper=True)
-        Q = Q @ Rinv
+        if out is None:
+            target = torch.empty_like(Q)
+        else:
+            target = out if p == passes - 1 else W
+        Q = _update(target, 0.0, None, Q, Rinv, dense=dense)
         R = Rp if R is None else Rp @ R
     return Q, R
 
 
-def lanczos_step(apply: Callable[[], None], Q, W, Qp, Bp, A_out, B_out, lean: bool = False) -> None:
+def lanczos_step(apply: Callable[[], None], Q, W, Qp, Bp, A_out, B_out, lean: bool = False,
+                 dense=None) -> None:
     """One block-Lanczos step on preallocated tensors ([S, D, k] blocks, [S, k, k] coefficients).
 
     `apply()` must compute W = H Q in place.  On return Q holds Q_{j+1}, Qp holds Q_j,
-    Bp = B_out = B_j and A_out = A_j.  Everything is stream-ordered (no host synchronisation), so
-    the step can be captured in a CUDA graph.  lean=True skips the local re-orthogonalisation
-    and uses one Cholesky-QR pass: 5 tall-skinny products per step instead of 9 (they are FP64
-    bound on GB300)."""
+    Bp = B_out = B_j and A_out = A_j; W is scratch.  Everything is stream-ordered (no host
+    synchronisation), so the step can be captured in a CUDA graph.  lean=True skips the local
+    re-orthogonalisation and uses one Cholesky-QR pass: 5 tall-skinny products per step
+    instead of 9."""
     apply()
-    A = _gram(Q, W)
-    W.baddbmm_(Q, A, beta=1.0, alpha=-1.0)
-    W.baddbmm_(Qp, Bp.mH, beta=1.0, alpha=-1.0)
+    A = _gram(Q, W, dense)
+    _update(W, 1.0, W, Q, -A, Qp, -Bp.mH, dense=dense)  # W -= Q A + Q_{j-1} B_{j-1}^H
     if not lean:
-        C = _gram(Q, W)  # local re-orthogonalisation against the current block
-        W.baddbmm_(Q, C, beta=1.0, alpha=-1.0)
+        C = _gram(Q, W, dense)  # local re-orthogonalisation against the current block
+        _update(W, 1.0, W, Q, -C, dense=dense)
         A = A + C
     A = 0.5 * (A + A.mH)
-    Qn, B = _cholqr(W, passes=1 if lean else 2)
     Qp.copy_(Q)
-    Q.copy_(Qn)
+    _, B = _cholqr(W, passes=1 if lean else 2, dense=dense, out=Q)
     Bp.copy_(B)
     A_out.copy_(A)
     B_out.copy_(B)
@@ -107,7 +184,7 @@ def block_tridiagonal(A: List, B: List):
 
 
 def block_lanczos(apply: Callable[[], None], Q, W, steps: int, graph: bool = False,
-                  timer: Optional[dict] = None, lean: bool = False):
+                  timer: Optional[dict] = None, lean: bool = False, dense=None):
     """Runs `steps` block-Lanczos steps with W = H Q computed by `apply()`; Q must hold an
     orthonormal starting block.  Returns the eigenvalues of T per sector ([S, steps * k],
     ascending).  With graph=True one step is captured in a CUDA graph after a warm-up step
@@ -131,12 +208,12 @@ def block_lanczos(apply: Callable[[], None], Q, W, steps: int, graph: bool = Fal
         side = torch.cuda.Stream(Q.device)
         side.wait_stream(torch.cuda.current_stream(Q.device))
         with torch.cuda.stream(side):
-            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur, lean)  # step 0, also the warm-up
+            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur, lean, dense)  # step 0, also the warm-up
         torch.cuda.current_stream(Q.device).wait_stream(side)
         record()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
-            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur, lean)
+            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur, lean, dense)
         # capture does not execute: step 1 runs at the first replay below
     start = end = None
     if timer is not None and Q.is_cuda:
@@ -149,7 +226,7 @@ def block_lanczos(apply: Callable[[], None], Q, W, steps: int, graph: bool = Fal
         if g is not None:
             g.replay()
         else:
-            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur, lean)
+            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur, lean, dense)
         record()
     if start is not None:
         end.record()
@@ -160,7 +237,7 @@ def block_lanczos(apply: Callable[[], None], Q, W, steps: int, graph: bool = Fal
     return torch.linalg.eigvalsh(T)
 
 
-def random_start(batch, seed: int = 0):
+def random_start(batch, seed: int = 0, dense=None):
     """Fills batch.X with an orthonormal random block per sector (zero padding rows)."""
     import torch
 
@@ -171,22 +248,23 @@ def random_start(batch, seed: int = 0):
             1j * torch.randn((d, batch.k), dtype=torch.float64, generator=gen)
         batch.X[s].zero_()
         batch.X[s, :d].copy_(x.to(torch.complex128))
-    Q, _ = _cholqr(batch.X)
+    Q, _ = _cholqr(batch.X, dense=dense)
     batch.X.copy_(Q)
     return batch.X
 
 
 def sector_ground_states(batch, steps: int, seed: int = 0, graph: bool = True,
-                         timer: Optional[dict] = None, lean: bool = False) -> np.ndarray:
+                         timer: Optional[dict] = None, lean: bool = False, dense=None) -> np.ndarray:
     """Lowest eigenvalue of every sector of a SectorBatch after `steps` block-Lanczos steps."""
-    random_start(batch, seed)
-    ev = block_lanczos(lambda: batch.run(), batch.X, batch.Y, steps, graph=graph, timer=timer, lean=lean)
+    random_start(batch, seed, dense)
+    ev = block_lanczos(lambda: batch.run(), batch.X, batch.Y, steps, graph=graph, timer=timer, lean=lean,
+                       dense=dense)
     batch.check_errors()
     return ev[:, 0].cpu().numpy()
 
 
 def ground_state(apply: Callable[[], None], Q, W, steps: int, graph: bool = False,
-                 timer: Optional[dict] = None):
+                 timer: Optional[dict] = None, dense=None):
     """Lowest eigenpair by block Lanczos with the Krylov blocks kept for the Ritz vector.
 
     Q, W: [1, D, k] blocks (Q orthonormal on entry), `apply()` computes W = H Q.  Returns
@@ -210,7 +288,7 @@ def ground_state(apply: Callable[[], None], Q, W, steps: int, graph: bool = Fals
         B_hist.append(B_cur.clone())
 
     def eager():
-        lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur)
+        lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur, dense=dense)
 
     g = None
     if graph and Q.is_cuda:
@@ -218,13 +296,13 @@ def ground_state(apply: Callable[[], None], Q, W, steps: int, graph: bool = Fals
         side.wait_stream(torch.cuda.current_stream(Q.device))
         with torch.cuda.stream(side):
             blocks.append(Q[0].clone())
-            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur)
+            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur, dense=dense)
         torch.cuda.current_stream(Q.device).wait_stream(side)
         A_hist.append(A_cur.clone())
         B_hist.append(B_cur.clone())
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
-            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur)
+            lanczos_step(apply, Q, W, Qp, Bp, A_cur, B_cur, dense=dense)
     start = end = None
     if timer is not None and Q.is_cuda:
         torch.cuda.synchronize(Q.device)
@@ -258,7 +336,7 @@ def _energy_function():
         products or one matvec per coupling."""
 
         @staticmethod
-        def forward(ctx, theta, pop, k, steps, seed, graph):
+        def forward(ctx, theta, pop, k, steps, seed, graph, dense):
             import numpy as np
             pop.set_theta(theta.detach().cpu().numpy())
             op = pop.operator
@@ -267,14 +345,14 @@ def _energy_function():
             gen = torch.Generator(device="cpu").manual_seed(seed)
             Q = (torch.randn((1, D, k), generator=gen, dtype=torch.float64)
                  + 1j * torch.randn((1, D, k), generator=gen, dtype=torch.float64)).to(dev)
-            Q, _ = _cholqr(Q)
+            Q, _ = _cholqr(Q, dense=dense)
             W = torch.empty_like(Q)
             Q = Q.contiguous()
 
             def apply():
                 op.apply_device(Q[0], out=W[0], check=False)
 
-            e0, psi = ground_state(apply, Q, W, steps, graph=graph)
+            e0, psi = ground_state(apply, Q, W, steps, graph=graph, dense=dense)
             op.check_errors()
             ctx.pop = pop
             ctx.psi = psi
@@ -285,7 +363,8 @@ def _energy_function():
         def backward(ctx, grad):
             (theta,) = ctx.saved_tensors
             hf = ctx.pop.coupling_products(ctx.psi, ctx.psi).real
-            return (grad.to(hf.device) * hf).to(dtype=theta.dtype, device=theta.device), None, None, None, None, None
+            return ((grad.to(hf.device) * hf).to(dtype=theta.dtype, device=theta.device),
+                    None, None, None, None, None, None)
 
     return GroundStateEnergy
 
@@ -293,7 +372,8 @@ def _energy_function():
 _GSE = None
 
 
-def ground_state_energy(pop, theta, k: int = 8, steps: int = 60, seed: int = 0, graph: bool = True):
+def ground_state_energy(pop, theta, k: int = 8, steps: int = 60, seed: int = 0, graph: bool = True,
+                        dense=None):
     """E0(theta) of a ParametrizedOperator by k-RHS block Lanczos, differentiable in theta."""
     import torch
 
@@ -302,4 +382,4 @@ def ground_state_energy(pop, theta, k: int = 8, steps: int = 60, seed: int = 0, 
         _GSE = _energy_function()
     if not isinstance(theta, torch.Tensor):
         theta = torch.as_tensor(theta, dtype=torch.float64)
-    return _GSE.apply(theta, pop, k, steps, seed, graph)
+    return _GSE.apply(theta, pop, k, steps, seed, graph, dense)
