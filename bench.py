@@ -531,7 +531,11 @@ def run_sectors(args):
     for s, d in enumerate(sizes):
         xs = rng.normal(size=(d, k)) + 1j * rng.normal(size=(d, k))
         batch.X[s, :d].copy_(torch.from_numpy(xs))
+    # the plan's autotuner: one persistent launch over all sectors, or one launch per sector
+    tune = batch.autotune()
     batch.capture()
+    # kernels per run: the prescaled pair copy of X + the matvec, once or per sector
+    launches_per_run = 2 if tune["batched"] else 2 * len(ops)
     stream = torch.cuda.current_stream()
     for _ in range(args.warmup):
         batch.replay()
@@ -551,8 +555,24 @@ def run_sectors(args):
         print(json.dumps({"metric": "H*x matrix elements/s", "value": value, "unit": "elements/s", "n_gpus": 1,
                           "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms,
                           "config": {"workload": args.config, "sectors": len(ops), "states": sum(sizes),
-                                     "nnz": sum(nnzs), "rhs": k}, "gpu_launches": args.steps}))
+                                     "nnz": sum(nnzs), "rhs": k, "form": "batched" if tune["batched"] else
+                                     "per-sector launches"}, "gpu_launches": launches_per_run * args.steps}))
         return 0
+    # the same launch with FP64 multiply-adds instead of FP32 pairs, and the difference it makes
+    ls.Operator.block_arithmetic("fp64")
+    batch.run()
+    torch.cuda.synchronize()
+    start.record(stream)
+    for _ in range(2):
+        batch.run()
+    end.record(stream)
+    torch.cuda.synchronize()
+    t_fp64_block = start.elapsed_time(end) / 2
+    y_fp64 = batch.Y.clone()
+    ls.Operator.block_arithmetic("pairs")
+    batch.run(check=True)
+    pair_rel_l2 = float(torch.linalg.vector_norm(batch.Y - y_fp64) / torch.linalg.vector_norm(y_fp64))
+    del y_fp64
     # the same work as one launch per sector (no batching across sectors, no graph)
     start.record(stream)
     for s, op in enumerate(ops):
@@ -623,9 +643,14 @@ def run_sectors(args):
                    "l2": "inputs larger than L2 (X, Y {:.2f} GB each)".format(batch.X.numel() * 16 / 1e9)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_source": peak_kind, "bytes_per_launch": bytes_per_launch},
-        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps, "clocks": clocks.summary(),
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_run * args.steps, "clocks": clocks.summary(),
         "basis_build_s": t_build,
-        "extra": {"per_sector_launches_ms": t_loop, "batched_speedup_vs_per_sector": t_loop / t_ms,
+        "extra": {"form": "one persistent launch over all sectors" if tune["batched"] else
+                  "one launch per sector (in the CUDA graph)",
+                  "autotune_ms": {"batched": tune["ms_batched"], "per_sector": tune["ms_per_sector"]},
+                  "block_arithmetic": "FP32 pairs", "fp64_block_arithmetic_ms": t_fp64_block,
+                  "pairs_vs_fp64_rel_l2": pair_rel_l2,
+                  "per_sector_launches_ms": t_loop, "batched_speedup_vs_per_sector": t_loop / t_ms,
                   "plain_one_vector_all_sectors_ms": t_plain,
                   "speedup_per_vector_vs_plain": t_plain * k / t_ms,
                   "lanczos": {"steps": c["lanczos_steps"], "ms_per_step": timer["ms"] / timer["steps"],

@@ -349,8 +349,9 @@ int ls_gpu_set_enumeration_rule(int exact);
  * Hamiltonian in different momentum / inversion sectors of one group), each chunk of up to 16
  * right-hand sides is ONE persistent kernel launch over the rows of all sectors, so uneven sector
  * sizes balance across the GPU; otherwise the plan launches the sectors one after the other
- * (ls_gpu_sector_plan_is_batched tells which).  Running a plan allocates nothing and does not
- * synchronise: it may be captured in a CUDA graph (make one uncaptured run first).  A plan keeps
+ * (ls_gpu_sector_plan_is_batched tells which form runs).  Running a plan does not synchronise and
+ * allocates only stream-ordered (cudaMallocAsync / cudaFreeAsync of the copy of x scaled by the
+ * orbit norms), so it may be captured in a CUDA graph (make one uncaptured run first).  A plan keeps
  * device pointers of the operators' uploaded tables: changing an operator's terms invalidates it
  * (run then fails).  Errors of generated states (wrong particle number) go to the device error
  * word: check with ls_gpu_check_errors. */
@@ -359,6 +360,15 @@ int ls_gpu_sector_plan_create(int n_sectors, ls_hs_operator const *const *ops, i
                               int64_t ldy, int adjoint, void **plan);
 int ls_gpu_sector_plan_run(void const *plan, void *stream);
 int ls_gpu_sector_plan_is_batched(void const *plan);
+/* Chooses the form: batched != 0 runs one launch per chunk over all sectors (LS_GPU_ERR_INVALID
+ * if the sectors cannot share one), 0 one launch per sector. */
+int ls_gpu_sector_plan_set_batched(void *plan, int batched);
+/* Times both forms on `stream` (one warm-up and two timed runs each; they overwrite the output
+ * blocks) and keeps the faster: one persistent launch wins for many small sectors, one launch per
+ * sector can win for a few large ones.  Reports the choice and both times (ms per run; -1 for a
+ * form the plan cannot run). */
+int ls_gpu_sector_plan_autotune(void *plan, void *stream, int *batched, double *ms_batched,
+                                double *ms_per_sector);
 int ls_gpu_sector_plan_destroy(void *plan);
 
 /* One-shot form of the above (leading dimension k); synchronises `stream` before returning. */
@@ -397,6 +407,16 @@ int ls_gpu_enumerate_noalloc(ls_hs_basis const *basis, uint64_t *d_out, int64_t 
  * (320, 8).  The fallback kernel for groups whose packed tables do not fit (or 64-bit states)
  * always runs 256-thread CTAs. */
 int ls_gpu_set_matvec_config(int threads_per_block, int waves);
+/* Arithmetic of complex blocks of 8 or 16 right-hand sides in the plain and the batched
+ * multi-sector kernels: 1 (default) = FP32 pairs, 0 = FP64.  In the pair form x_j * n_j is stored once per
+ * call as two floats per component (16 bytes per complex element, like complex128), the
+ * coefficient of each element is formed in FP64 and split, and the multiply-adds run on the
+ * FP32 pipe with error-free products and two-sum accumulation (about 2^-46 relative per product;
+ * H X agrees with the FP64 form to ~1e-14 relative).  With 16 columns the FP64 form is bound by
+ * GB300's FP64 pipe (4 FP64 FMAs per element and column).  One right-hand side, real vectors
+ * and blocks of 4 always run in FP64.  Returns LS_GPU_ERR_INVALID for other values. */
+int ls_gpu_set_block_arithmetic(int pairs);
+int ls_gpu_get_block_arithmetic(void);
 /* Most right-hand sides per kernel launch (16, 8, 4 or 1; larger k is split into launches). */
 int ls_gpu_set_matvec_rhs_tile(int rhs_tile);
 int ls_gpu_get_matvec_config(int *threads_per_block, int *waves, int *rhs_tile);

@@ -755,6 +755,18 @@ class Operator(_LinearOperator):
         return th.value, wv.value, ms.value
 
     @staticmethod
+    def block_arithmetic(mode: Optional[str] = None) -> str:
+        """Arithmetic of complex blocks of 8 or 16 right-hand sides: "pairs" (default: FP32-pair
+        multiply-adds from an FP64 coefficient and a prescaled pair copy of x, ~1e-14 relative to
+        the FP64 form) or "fp64".  Sets it when `mode` is given; returns the mode in force."""
+        lib = N.lib()
+        if mode is not None:
+            if mode not in ("pairs", "fp64"):
+                raise ValueError("block arithmetic is 'pairs' or 'fp64'")
+            N.check(lib.ls_gpu_set_block_arithmetic(1 if mode == "pairs" else 0), "block arithmetic")
+        return "pairs" if lib.ls_gpu_get_block_arithmetic() == 1 else "fp64"
+
+    @staticmethod
     def launch_config():
         """(threads per block, grid waves, right-hand-side tile) used by the matvec kernels."""
         th, wv, tile = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
@@ -844,6 +856,27 @@ class SectorBatch:
         if check:
             N.check(self._lib.ls_gpu_check_errors(stream), "sector matvec")
         return self.Y
+
+    def autotune(self, stream=None) -> dict:
+        """Times the batched form (one launch over all sectors) against one launch per sector and
+        keeps the faster (recapture afterwards: a recorded graph keeps the form it recorded).
+        Returns {"batched": bool, "ms_batched": t, "ms_per_sector": t}."""
+        import torch
+
+        if stream is None:
+            stream = torch.cuda.current_stream(self.device).cuda_stream
+        b, tb, tp = ctypes.c_int(0), c_double(0.0), c_double(0.0)
+        N.check(self._lib.ls_gpu_sector_plan_autotune(self._plan, stream, byref(b), byref(tb), byref(tp)),
+                "sector plan autotune")
+        self.batched = bool(b.value)
+        self._graph = None
+        return {"batched": self.batched, "ms_batched": tb.value, "ms_per_sector": tp.value}
+
+    def set_batched(self, batched: bool) -> None:
+        """Forces the form: one launch over all sectors (True) or one launch per sector."""
+        N.check(self._lib.ls_gpu_sector_plan_set_batched(self._plan, int(bool(batched))), "sector plan form")
+        self.batched = bool(batched)
+        self._graph = None
 
     def capture(self):
         """Records run() in a CUDA graph (after one uncaptured run that uploads every table)."""

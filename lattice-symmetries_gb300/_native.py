@@ -182,6 +182,11 @@ _SIGNATURES = [
     ("ls_gpu_autotune_matvec", c_int, [POINTER(ls_hs_operator), c_int, POINTER(c_int), POINTER(c_int),
                                        POINTER(c_double)]),
     ("ls_gpu_count_nonzeros", c_int, [POINTER(ls_hs_operator), POINTER(c_int64)]),
+    ("ls_gpu_sector_plan_set_batched", c_int, [c_void_p, c_int]),
+    ("ls_gpu_sector_plan_autotune", c_int, [c_void_p, c_void_p, POINTER(c_int), POINTER(c_double),
+                                            POINTER(c_double)]),
+    ("ls_gpu_set_block_arithmetic", c_int, [c_int]),
+    ("ls_gpu_get_block_arithmetic", c_int, []),
     ("ls_gpu_block_gram", c_int, [c_int64, c_int64, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("ls_gpu_block_update", c_int, [c_int64, c_int64, c_int, c_double, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_void_p, c_void_p]),

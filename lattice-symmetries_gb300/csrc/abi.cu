@@ -19,6 +19,8 @@ namespace lsg {
 int set_matvec_config(int threads, int blocks_per_sm);
 int set_matvec_rhs_tile(int tile);
 void get_matvec_config(int* threads, int* waves, int* rhs_tile);
+int set_block_arithmetic(int pairs);
+int get_block_arithmetic();
 }
 
 using namespace lsg;
@@ -252,6 +254,17 @@ extern "C" int ls_gpu_set_matvec_rhs_tile(int rhs_tile) {
   std::lock_guard<std::mutex> lock(g_mutex);
   const int rc = set_matvec_rhs_tile(rhs_tile);
   return rc != 0 ? fail(rc, "the right-hand-side tile must be 1, 4, 8 or 16") : 0;
+}
+
+extern "C" int ls_gpu_set_block_arithmetic(int pairs) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (set_block_arithmetic(pairs) != 0) return fail(LS_GPU_ERR_INVALID, "block arithmetic: 1 = FP32 pairs, 0 = FP64");
+  return 0;
+}
+
+extern "C" int ls_gpu_get_block_arithmetic(void) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  return get_block_arithmetic();
 }
 
 extern "C" int ls_gpu_get_matvec_config(int* threads_per_block, int* waves, int* rhs_tile) {
@@ -1557,6 +1570,58 @@ extern "C" int ls_gpu_sector_plan_run(void const* plan, void* stream) {
       return fail(LS_GPU_ERR_INVALID, "an operator of the sector plan changed after the plan was created");
   }
   return sector_plan_run(h->plan, device_error_word(), (cudaStream_t)stream);
+}
+
+extern "C" int ls_gpu_sector_plan_set_batched(void* plan, int batched) {
+  SectorPlanHandle* h = (SectorPlanHandle*)plan;
+  if (h == nullptr || h->magic != kPlanMagic) return fail(LS_GPU_ERR_INVALID, "not a sector plan");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (sector_plan_set_batched(h->plan, batched != 0) != 0)
+    return fail(LS_GPU_ERR_INVALID, "the sectors of this plan cannot share one launch");
+  return 0;
+}
+
+extern "C" int ls_gpu_sector_plan_autotune(void* plan, void* stream, int* batched, double* ms_batched,
+                                           double* ms_per_sector) {
+  SectorPlanHandle* h = (SectorPlanHandle*)plan;
+  if (h == nullptr || h->magic != kPlanMagic) return fail(LS_GPU_ERR_INVALID, "not a sector plan");
+  cudaStream_t s = (cudaStream_t)stream;
+  double t[2] = {-1.0, -1.0};  // [per sector, batched]
+  bool can_batch = false;
+  {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    can_batch = sector_plan_set_batched(h->plan, true) == 0;
+  }
+  for (int form = can_batch ? 1 : 0; form >= 0; --form) {
+    {
+      std::lock_guard<std::mutex> lock(g_mutex);
+      sector_plan_set_batched(h->plan, form == 1);
+    }
+    int rc = ls_gpu_sector_plan_run(plan, stream);  // warm-up (uploads, first-touch)
+    if (rc != 0) return rc;
+    cudaEvent_t e0, e1;
+    if (!cuda_ok(cudaEventCreate(&e0), "event") || !cuda_ok(cudaEventCreate(&e1), "event")) return LS_GPU_ERR_CUDA;
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < 2 && rc == 0; ++r) rc = ls_gpu_sector_plan_run(plan, stream);
+    cudaEventRecord(e1, s);
+    const bool ok = cuda_ok(cudaEventSynchronize(e1), "autotune sector plan");
+    float ms = 0.0f;
+    if (ok) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != 0) return rc;
+    if (!ok) return LS_GPU_ERR_CUDA;
+    t[form] = ms / 2.0;
+  }
+  const bool use = can_batch && t[1] <= t[0];
+  {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    sector_plan_set_batched(h->plan, use);
+  }
+  if (batched) *batched = use ? 1 : 0;
+  if (ms_batched) *ms_batched = t[1];
+  if (ms_per_sector) *ms_per_sector = t[0];
+  return 0;
 }
 
 extern "C" int ls_gpu_sector_plan_destroy(void* plan) {

@@ -23,6 +23,7 @@
 // No reference counterpart: the reference's eigensolvers are scipy's eigsh over the matvec
 // (python/lattice_symmetries/__init__.py:751-752) and PRIMME (chapel/src/Diagonalize.chpl).
 #include "lsg.h"
+#include "pairs.cuh"
 
 #include <algorithm>
 
@@ -32,72 +33,6 @@ namespace {
 constexpr int kMaxK = 16;      // columns per block handled by these kernels
 constexpr int kThreads = 256;  // threads per CTA
 constexpr int kTileRows = 32;  // rows of X / Y staged per tile (Gram)
-
-struct F2 {
-  float h, l;
-};
-
-// hi + lo split of a double: hi = its top 24 significant bits (exact), lo = the next bits
-// rounded to 24.  Magnitudes below 2^-126 become 0, magnitudes from 2^128 on become +-inf,
-// NaN stays NaN.
-__device__ __forceinline__ F2 split_double(double a) {
-  const unsigned long long u = (unsigned long long)__double_as_longlong(a);
-  const unsigned hw = (unsigned)(u >> 32);
-  const unsigned sign = hw & 0x80000000u;
-  const int e = (int)((hw >> 20) & 0x7ffu);
-  const unsigned mant23 = (unsigned)(u >> 29) & 0x7fffffu;
-  F2 r;
-  if (e <= 896) {
-    r.h = __uint_as_float(sign);
-    r.l = 0.0f;
-    return r;
-  }
-  if (e >= 1151) {
-    const bool nan = e == 2047 && (u & 0xfffffffffffffull) != 0;
-    r.h = __uint_as_float(sign | 0x7f800000u | (nan ? 0x400000u : 0u));
-    r.l = 0.0f;
-    return r;
-  }
-  const unsigned ebits = (unsigned)(e - 896) << 23;  // 2^(e - 1023) as a float exponent field
-  r.h = __uint_as_float(sign | ebits | mant23);
-  const unsigned low = (unsigned)u & 0x1fffffffu;    // remaining 29 bits, weight 2^(e - 1075)
-  const float lo = __fmul_rn(__fmul_rn(__uint2float_rn(low), 0x1p-52f), __uint_as_float(ebits));
-  r.l = __uint_as_float(__float_as_uint(lo) ^ sign);
-  return r;
-}
-
-// Exact float -> double by bit manipulation (subnormal floats become 0).
-__device__ __forceinline__ double float_bits_to_double(float f) {
-  const unsigned b = __float_as_uint(f);
-  const unsigned e = (b >> 23) & 0xffu;
-  const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
-  const unsigned long long m = (unsigned long long)(b & 0x7fffffu) << 29;
-  if (e == 0) return __longlong_as_double((long long)sign);
-  if (e == 255) return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull | m));
-  return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 896) << 52) | m));
-}
-
-__device__ __forceinline__ double join(F2 v) { return float_bits_to_double(v.h) + float_bits_to_double(v.l); }
-
-// acc += a * b.  The hi*hi product is error-free (fmaf), the cross terms are first order, the
-// sum is a two-sum.  Explicit _rn intrinsics keep the compiler from contracting the
-// error-free transformations into FMAs.
-__device__ __forceinline__ void mac(F2& acc, const float ah, const float al, const float bh, const float bl) {
-  const float p = __fmul_rn(ah, bh);
-  float e = __fmaf_rn(ah, bh, -p);
-  e = __fmaf_rn(ah, bl, e);
-  e = __fmaf_rn(al, bh, e);
-  const float t = __fadd_rn(acc.h, p);
-  const float bp = __fsub_rn(t, acc.h);
-  const float err = __fadd_rn(__fsub_rn(acc.h, __fsub_rn(t, bp)), __fsub_rn(p, bp));
-  acc.l = __fadd_rn(acc.l, __fadd_rn(err, e));
-  acc.h = t;
-}
-
-__device__ __forceinline__ float4 split_c(double2 v) {
-  const F2 re = split_double(v.x), im = split_double(v.y);
-  return make_float4(re.h, re.l, im.h, im.l);
-}
 
 // Partial Gram matrices: CTA (c, s) sums conj(X[s, r, i]) Y[s, r, j] over its rows.
 // Thread o < k*k of row group g owns output (i, j) = (o / k, o % k) for rows r = g (mod groups).

@@ -232,7 +232,8 @@ int sector_plan_build(const std::vector<MatvecProblem>& problems, bool shareable
                       const std::vector<const double*>& xs, int64_t ldx, const std::vector<double*>& ys,
                       int64_t ldy, SectorPlan** out);
 int sector_plan_run(const SectorPlan* plan, int* d_err, cudaStream_t s);
-bool sector_plan_batched(const SectorPlan* plan);
+bool sector_plan_batched(const SectorPlan* plan);            // runs as one launch per RHS chunk
+int sector_plan_set_batched(SectorPlan* plan, bool batched);  // LS_GPU_ERR_INVALID if it cannot
 void sector_plan_free(SectorPlan* plan);
 
 // Per-state term application on device batches (apply.cu), the semantics of

@@ -51,6 +51,17 @@ int set_matvec_rhs_tile(int tile) {
   return 0;
 }
 
+// Complex blocks of 8 or 16 right-hand sides accumulate in FP32 pairs (1) or in FP64 (0).
+static int g_block_pairs = 1;
+
+int set_block_arithmetic(int pairs) {
+  if (pairs != 0 && pairs != 1) return LS_GPU_ERR_INVALID;
+  g_block_pairs = pairs;
+  return 0;
+}
+
+int get_block_arithmetic() { return g_block_pairs; }
+
 void get_matvec_config(int* threads, int* waves, int* rhs_tile) {
   if (threads) *threads = g_threads_override > 0 ? g_threads_override : 320;
   if (waves) *waves = g_blocks_per_sm_override > 0 ? g_blocks_per_sm_override : 8;
@@ -70,6 +81,19 @@ __global__ void k_prescale(const double* __restrict__ x, int64_t ldx, const doub
   }
 }
 
+// xp[i][c] = x[i][c] * norms[i] as a float pair per component [re_h, re_l, im_h, im_l] for k
+// complex columns (the gather source of the pair kernels).
+__global__ void k_prescale_pairs(const double2* __restrict__ x, int64_t ldx, const double* __restrict__ norms,
+                                 int64_t n, int k, float4* __restrict__ xp) {
+  const int64_t total = n * k;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / k, c = e - i * k;
+    const double nrm = __ldg(norms + i);
+    const double2 v = __ldg(x + i * ldx + c);
+    const F2 re = split_double(v.x * nrm), im = split_double(v.y * nrm);
+    xp[e] = make_float4(re.h, re.l, im.h, im.l);
+  }
+}
 
 constexpr size_t kMaxDynamicSmem = 200 * 1024;
 
@@ -98,39 +122,76 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
     const PackedLayout PL = make_packed_layout(p);
     const bool packed = p.group.gpl > 0 && p.group.onehot_packed != nullptr && PL.total <= kMaxDynamicSmem;
     if (packed) {
-      // Gather source x_j * n_j for all k columns (one streaming pass), so that the kernels read
-      // no norm per generated element.  Not when counting elements (the count needs the norms).
-      MatvecProblem q = p;
-      double* d_xs = nullptr;
-      const size_t xs_bytes = (size_t)p.n_rows * k * scalar_words * sizeof(double);
-      if (p.nnz_counter == nullptr && p.index.norms != nullptr &&
-          cudaMallocAsync((void**)&d_xs, xs_bytes, s) == cudaSuccess) {
-        const int64_t total = p.n_rows * k * (int64_t)scalar_words;
-        const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 16));
-        k_prescale<<<blocks, 256, 0, s>>>(d_x, ldx, p.index.norms, p.n_rows, k, (int)scalar_words, d_xs);
-        if (!cuda_ok(cudaGetLastError(), "k_prescale")) {
-          cudaFreeAsync(d_xs, s);
-          return LS_GPU_ERR_CUDA;
-        }
-      } else {
-        cudaGetLastError();  // a failed stream-ordered allocation: gather x and the norms instead
-        d_xs = nullptr;
-      }
-      int done = 0, rc = 0;
-      while (done < k && rc == 0) {
+      // Right-hand-side chunks of 16, 8, 4 and 1 columns; complex chunks of 8 or 16 run the
+      // FP32-pair kernels (g_block_pairs).
+      std::vector<int> chunks;
+      for (int done = 0; done < k;) {
         const int left = k - done;
         const int most = std::min(left, g_rhs_tile);
         int chunk = most >= 16 ? 16 : most >= 8 ? 8 : most >= 4 ? 4 : 1;
         if (!cplx && left == 2 && g_rhs_tile >= 2) chunk = 2;
         if (p.group.fermionic && !cplx) chunk = 1;  // fermionic real path: one column per launch
+        chunks.push_back(chunk);
+        done += chunk;
+      }
+      // Gather sources x_j * n_j for all k columns (one streaming pass each), so that the kernels
+      // read no norm per generated element: FP64 for the FP64 kernels, float pairs for the pair
+      // kernels.  Not when counting elements (the count needs the norms).
+      const bool can_prescale = p.nnz_counter == nullptr && p.index.norms != nullptr;
+      const bool want_pairs = can_prescale && cplx && g_block_pairs != 0 &&
+                              std::any_of(chunks.begin(), chunks.end(), [](int c) { return c >= 8; });
+      const bool want_fp64 = can_prescale && std::any_of(chunks.begin(), chunks.end(), [&](int c) {
+                               return !(want_pairs && c >= 8);
+                             });
+      const int64_t total_elems = p.n_rows * (int64_t)k;
+      const int pre_blocks = (int)std::max<int64_t>(
+          1, std::min<int64_t>((total_elems * (int64_t)scalar_words + 255) / 256, (int64_t)num_sms() * 16));
+      double* d_xs = nullptr;
+      float4* d_xp = nullptr;
+      if (want_fp64) {
+        if (cudaMallocAsync((void**)&d_xs, (size_t)total_elems * scalar_words * sizeof(double), s) == cudaSuccess) {
+          k_prescale<<<pre_blocks, 256, 0, s>>>(d_x, ldx, p.index.norms, p.n_rows, k, (int)scalar_words, d_xs);
+          if (!cuda_ok(cudaGetLastError(), "k_prescale")) {
+            cudaFreeAsync(d_xs, s);
+            return LS_GPU_ERR_CUDA;
+          }
+        } else {
+          cudaGetLastError();  // a failed stream-ordered allocation: gather x and the norms instead
+          d_xs = nullptr;
+        }
+      }
+      if (want_pairs) {
+        if (cudaMallocAsync((void**)&d_xp, (size_t)total_elems * sizeof(float4), s) == cudaSuccess) {
+          k_prescale_pairs<<<pre_blocks, 256, 0, s>>>(reinterpret_cast<const double2*>(d_x), ldx, p.index.norms,
+                                                      p.n_rows, k, d_xp);
+          if (!cuda_ok(cudaGetLastError(), "k_prescale_pairs")) {
+            cudaFreeAsync(d_xp, s);
+            if (d_xs) cudaFreeAsync(d_xs, s);
+            return LS_GPU_ERR_CUDA;
+          }
+        } else {
+          cudaGetLastError();  // no room for the pair copy: the FP64 kernels gather x and the norms
+          d_xp = nullptr;
+        }
+      }
+      MatvecProblem q = p;
+      q.ldxs = k;
+      int done = 0, rc = 0;
+      for (const int chunk : chunks) {
         const double* xs = d_x + (size_t)done * scalar_words;
         double* ys = d_y + (size_t)done * scalar_words;
-        q.xs = d_xs ? d_xs + (size_t)done * scalar_words : nullptr;
-        q.ldxs = k;
-        rc = launch_packed(cplx, chunk, p.group.gpl, inv, q, PL, sh, xs, ldx, ys, ldy, d_err, binom, s);
+        if (d_xp != nullptr && chunk >= 8) {
+          q.xs = reinterpret_cast<const double*>(d_xp + done);
+          rc = launch_packed_pair(chunk, p.group.gpl, inv, q, PL, sh, xs, ldx, ys, ldy, d_err, binom, s);
+        } else {
+          q.xs = d_xs ? d_xs + (size_t)done * scalar_words : nullptr;
+          rc = launch_packed(cplx, chunk, p.group.gpl, inv, q, PL, sh, xs, ldx, ys, ldy, d_err, binom, s);
+        }
+        if (rc != 0) break;
         done += chunk;
       }
       if (d_xs) cudaFreeAsync(d_xs, s);
+      if (d_xp) cudaFreeAsync(d_xp, s);
       return rc;
     }
     if (p.group.fermionic)
@@ -168,7 +229,8 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
 struct SectorPlan {
   int n_sectors = 0, k = 0;
   int64_t ldx = 0, ldy = 0;
-  bool batched = false;
+  bool batched = false;      // the sectors can share one launch
+  bool use_batched = true;   // ... and run() does so (else one launch per sector)
   MatvecProblem shared{};          // tables of the first sector (batched form)
   PackedLayout layout{};
   int64_t total_rows = 0;
@@ -239,10 +301,36 @@ int sector_plan_build(const std::vector<MatvecProblem>& problems, bool shareable
   return 0;
 }
 
-bool sector_plan_batched(const SectorPlan* plan) { return plan != nullptr && plan->batched; }
+bool sector_plan_batched(const SectorPlan* plan) { return plan != nullptr && plan->batched && plan->use_batched; }
+
+int sector_plan_set_batched(SectorPlan* plan, bool batched) {
+  if (plan == nullptr || (batched && !plan->batched)) return LS_GPU_ERR_INVALID;
+  plan->use_batched = batched;
+  return 0;
+}
+
+// Gather source of the pair kernels in a batched launch: xp[row_begin_s + i][c] = x_s[i][c] *
+// n_s[i] as float pairs, for every sector s (blockIdx.y) and all k complex columns.
+__global__ void k_prescale_pairs_sectors(const SectorDesc* __restrict__ desc, int n_sectors, int64_t total_rows,
+                                         int k, int64_t ldx, float4* __restrict__ xp) {
+  const int s = blockIdx.y;
+  const int64_t begin = desc[s].row_begin;
+  const int64_t n = (s + 1 < n_sectors ? desc[s + 1].row_begin : total_rows) - begin;
+  const double2* __restrict__ x = reinterpret_cast<const double2*>(desc[s].x);
+  const double* __restrict__ norms = desc[s].index.norms;
+  float4* __restrict__ out = xp + (size_t)begin * k;
+  const int64_t total = n * k;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / k, c = e - i * k;
+    const double nrm = __ldg(norms + i);
+    const double2 v = __ldg(x + i * ldx + c);
+    const F2 re = split_double(v.x * nrm), im = split_double(v.y * nrm);
+    out[e] = make_float4(re.h, re.l, im.h, im.l);
+  }
+}
 
 int sector_plan_run(const SectorPlan* plan, int* d_err, cudaStream_t s) {
-  if (!plan->batched) {
+  if (!plan->batched || !plan->use_batched) {
     for (int i = 0; i < plan->n_sectors; ++i) {
       const int rc = launch_matvec(plan->problems[i], Scalar::Complex, plan->k, plan->xs[i], plan->ldx,
                                    plan->ys[i], plan->ldy, d_err, s);
@@ -255,12 +343,42 @@ int sector_plan_run(const SectorPlan* plan, int* d_err, cudaStream_t s) {
   if (plan->total_rows == 0) return 0;
   const LaunchShape sh = packed_shape(plan->total_rows);
   const bool inv = plan->shared.group.spin_inversion != 0;
-  for (const SectorPlan::Chunk& c : plan->chunks) {
-    const int rc = launch_sectors(c.k, plan->shared.group.gpl, inv, plan->shared, plan->layout, sh, c.d_desc,
-                                  plan->n_sectors, plan->total_rows, plan->ldx, plan->ldy, d_err, binom, s);
-    if (rc != 0) return rc;
+  // chunks of 8 or 16 columns run the FP32-pair kernels from a prescaled pair copy of all
+  // sectors' columns (one streaming pass); the others gather x and the norms in FP64
+  float4* d_xp = nullptr;
+  const bool want_pairs = g_block_pairs != 0 && plan->shared.nnz_counter == nullptr &&
+                          std::any_of(plan->chunks.begin(), plan->chunks.end(),
+                                      [](const SectorPlan::Chunk& c) { return c.k >= 8; });
+  if (want_pairs) {
+    if (cudaMallocAsync((void**)&d_xp, (size_t)plan->total_rows * plan->k * sizeof(float4), s) == cudaSuccess) {
+      const int n = plan->n_sectors;
+      const int64_t per_sector = (plan->total_rows * plan->k + n - 1) / n;
+      const int bx = (int)std::max<int64_t>(1, std::min<int64_t>((per_sector + 255) / 256,
+                                                                 ((int64_t)num_sms() * 16 + n - 1) / n));
+      k_prescale_pairs_sectors<<<dim3((unsigned)bx, (unsigned)n), 256, 0, s>>>(
+          plan->chunks[0].d_desc, n, plan->total_rows, plan->k, plan->ldx, d_xp);
+      if (!cuda_ok(cudaGetLastError(), "k_prescale_pairs_sectors")) {
+        cudaFreeAsync(d_xp, s);
+        return LS_GPU_ERR_CUDA;
+      }
+    } else {
+      cudaGetLastError();  // no room for the pair copy: FP64 kernels
+      d_xp = nullptr;
+    }
   }
-  return 0;
+  int rc = 0;
+  for (const SectorPlan::Chunk& c : plan->chunks) {
+    if (d_xp != nullptr && c.k >= 8)
+      rc = launch_sectors_pair(c.k, plan->shared.group.gpl, inv, plan->shared, plan->layout, sh, c.d_desc,
+                               plan->n_sectors, plan->total_rows, plan->ldx, plan->ldy, d_err, binom,
+                               reinterpret_cast<const double*>(d_xp), plan->k, c.col, s);
+    else
+      rc = launch_sectors(c.k, plan->shared.group.gpl, inv, plan->shared, plan->layout, sh, c.d_desc,
+                          plan->n_sectors, plan->total_rows, plan->ldx, plan->ldy, d_err, binom, nullptr, 0, 0, s);
+    if (rc != 0) break;
+  }
+  if (d_xp) cudaFreeAsync(d_xp, s);
+  return rc;
 }
 
 void sector_plan_free(SectorPlan* plan) {

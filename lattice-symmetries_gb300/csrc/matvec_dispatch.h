@@ -46,7 +46,17 @@ int launch_packed_fermi(bool cplx, int k, int gpl, const MatvecProblem& p, const
 struct SectorDesc;
 int launch_sectors(int k, int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L, LaunchShape sh,
                    const SectorDesc* d_desc, int n_sectors, int64_t total_rows, int64_t ldx, int64_t ldy,
-                   int* err, const uint64_t* binom, cudaStream_t s);
+                   int* err, const uint64_t* binom, const double* xs_all, int64_t ldxs, int col, cudaStream_t s);
+// FP32-pair variant (k in {8, 16}); xs_all holds x_j * n_j of all sectors as float pairs.
+int launch_sectors_pair(int k, int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L, LaunchShape sh,
+                        const SectorDesc* d_desc, int n_sectors, int64_t total_rows, int64_t ldx, int64_t ldy,
+                        int* err, const uint64_t* binom, const double* xs_all, int64_t ldxs, int col,
+                        cudaStream_t s);
+// FP32-pair packed kernels (complex, k in {8, 16}; fermionic groups included); p.xs holds
+// x_j * n_j as float pairs.
+int launch_packed_pair(int k, int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L, LaunchShape sh,
+                       const double* x, int64_t ldx, double* y, int64_t ldy, int* err, const uint64_t* binom,
+                       cudaStream_t s);
 constexpr int kSectorMaxGpl = 4;
 constexpr int kMaxSectors = 256;
 

@@ -23,6 +23,7 @@
 #pragma once
 
 #include "lsg.h"
+#include "pairs.cuh"
 
 namespace lsg {
 
@@ -478,7 +479,13 @@ __device__ __forceinline__ PackedTables stage_packed(const MatvecProblem& p, con
 
 // One output row of the packed kernels (executed by a whole warp): y[row, 0..K) for the sector
 // described by (ix, chars, spin_inversion, x, y).
-template <int GPL, bool INV, bool CPLX, int K, bool FERMI = false>
+//
+// PAIR (complex blocks): xs holds x_j * n_j as (hi, lo) float pairs [re_h, re_l, im_h, im_l]
+// (16 bytes per element, like complex128) and the multiply-adds run in FP32-pair arithmetic
+// (pairs.cuh): the coefficient is formed in FP64 and split once per element; each lane's pair
+// sums are converted to FP64 before the cross-lane reduction.  With 16 right-hand sides the FP64
+// form is bound by GB300's narrow FP64 pipe (4 FP64 FMAs per element and column).
+template <int GPL, bool INV, bool CPLX, int K, bool FERMI = false, bool PAIR = false>
 __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbits, const DeviceIndex& ix,
                                            const double2* __restrict__ chars, const int spin_inversion,
                                            const DeviceConstraint& cons, const double* __restrict__ x,
@@ -538,18 +545,37 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
   for (int k = 0; k < GPL; ++k) ga[k] |= (uint64_t)(2 * (lane + 32 * k));
 
   double dre = 0.0, dim = 0.0;
-  for (int t = lane; t < T.nd; t += 32) {
-    if ((a & T.dm[t]) == T.dr[t]) {
-      const double2 v = T.dv[t];
-      const bool neg = __popcll(a & T.ds[t]) & 1;
-      dre += neg ? -v.x : v.x;
-      if constexpr (CPLX) dim += neg ? -v.y : v.y;
+  F2 dpr{0.0f, 0.0f}, dpi{0.0f, 0.0f};  // PAIR: the diagonal element as pairs
+  if constexpr (PAIR) {
+    for (int t = lane; t < T.nd; t += 32) {
+      if ((a & T.dm[t]) == T.dr[t]) {
+        const double2 v = T.dv[t];
+        const bool neg = __popcll(a & T.ds[t]) & 1;
+        const F2 vr = split_double(v.x), vi = split_double(v.y);
+        dpr = pair_add(dpr, neg ? pair_neg(vr) : vr);
+        dpi = pair_add(dpi, neg ? pair_neg(vi) : vi);
+      }
     }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      dpr = pair_add(dpr, pair_shfl_xor(dpr, d));
+      dpi = pair_add(dpi, pair_shfl_xor(dpi, d));
+    }
+  } else {
+    for (int t = lane; t < T.nd; t += 32) {
+      if ((a & T.dm[t]) == T.dr[t]) {
+        const double2 v = T.dv[t];
+        const bool neg = __popcll(a & T.ds[t]) & 1;
+        dre += neg ? -v.x : v.x;
+        if constexpr (CPLX) dim += neg ? -v.y : v.y;
+      }
+    }
+    dre = warp_sum(dre);
+    if constexpr (CPLX) dim = warp_sum(dim);
   }
-  dre = warp_sum(dre);
-  if constexpr (CPLX) dim = warp_sum(dim);
 
   Acc acc;
+  F2 pre{0.0f, 0.0f}, pim{0.0f, 0.0f};  // PAIR: this lane's pair sums
   unsigned found = 0;
   // Lane s of the warp owns the s-th generated element since the last flush: the winning key
   // (representative + group slot) and the term that generated it.  The element's coefficient,
@@ -587,6 +613,42 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
         fre = prescaled ? f.re : f.re * nj;
         fim = prescaled ? f.im : f.im * nj;
       }
+    }
+    if constexpr (PAIR) {
+      static_assert(CPLX && K >= 2, "pair accumulation is for complex blocks");
+      const F2 cr = split_double(fre), ci = split_double(fim);
+      // U passes at a time: their gathers are issued before the multiply-adds, so that U loads
+      // per lane are in flight (the pair arithmetic leaves the kernel latency-bound otherwise)
+      constexpr int U = 4;
+      const float4* __restrict__ xp = reinterpret_cast<const float4*>(xg);
+      for (int s0 = 0; s0 < nslot; s0 += U * Q) {
+        float4 xv[U];
+        unsigned ok = 0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int s = s0 + u * Q + q;
+          const int64_t js = __shfl_sync(FULL, j, s & 31);
+          const bool valid = s < nslot && js >= 0;
+          ok |= valid ? 1u << u : 0u;
+          xv[u] = valid ? __ldg(xp + js * ldg + rhs) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int src = (s0 + u * Q + q) & 31;
+          const float crh = __shfl_sync(FULL, cr.h, src), crl = __shfl_sync(FULL, cr.l, src);
+          const float cih = __shfl_sync(FULL, ci.h, src), cil = __shfl_sync(FULL, ci.l, src);
+          if (ok & (1u << u)) {
+            // (cr + i ci)(xr + i xi); real elements (warp-uniform) have ci = 0
+            mac(pre, crh, crl, xv[u].x, xv[u].y);
+            mac(pim, crh, crl, xv[u].z, xv[u].w);
+            if (!real_elements) {
+              mac(pre, -cih, -cil, xv[u].z, xv[u].w);
+              mac(pim, cih, cil, xv[u].x, xv[u].y);
+            }
+          }
+        }
+      }
+      return;
     }
     if (CPLX && real_elements) {
       // real matrix elements (warp-uniform branch): complex x times a real factor
@@ -677,6 +739,32 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
     }
   }
   if (nslot > 0) flush();
+  if constexpr (PAIR) {
+    // FP32-pair epilogue: lanes with the same column combine, then
+    // y = acc / n_a + diag x_a, all in pairs; two FP64 adds per output
+#pragma unroll
+    for (int d = 16; d >= K; d >>= 1) {
+      pre = pair_add(pre, pair_shfl_xor(pre, d));
+      pim = pair_add(pim, pair_shfl_xor(pim, d));
+    }
+    if (lane < K) {
+      const double2 xi = __ldg(reinterpret_cast<const double2*>(x) + row * ldx + lane);
+      const F2 inv = split_double(inv_na), xr = split_double(xi.x), xm = split_double(xi.y);
+      F2 orr{0.0f, 0.0f}, oim{0.0f, 0.0f};
+      mac(orr, pre, inv);
+      mac(orr, dpr, xr);
+      mac(orr, pair_neg(dpi), xm);
+      mac(oim, pim, inv);
+      mac(oim, dpr, xm);
+      mac(oim, dpi, xr);
+      reinterpret_cast<double2*>(y)[row * ldy + lane] = make_double2(join(orr), join(oim));
+    }
+    if (nnz_counter != nullptr) {
+      const unsigned total = __reduce_add_sync(FULL, found);
+      if (lane == 0 && total) atomicAdd(nnz_counter, (unsigned long long)total);
+    }
+    return;
+  }
   if (nnz_counter != nullptr) {
     const unsigned total = __reduce_add_sync(FULL, found);
     if (lane == 0 && total) atomicAdd(nnz_counter, (unsigned long long)total);
@@ -702,8 +790,10 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
   }
 }
 
-template <int GPL, bool INV, bool CPLX, int K, bool FERMI = false>
-__global__ void __launch_bounds__(320, 2)
+// Pair kernels on small groups hold few registers: three CTAs per SM (more warps to hide the
+// gathers' latency).
+template <int GPL, bool INV, bool CPLX, int K, bool FERMI = false, bool PAIR = false>
+__global__ void __launch_bounds__(320, (PAIR && GPL <= 2) ? 3 : 2)
     k_matvec_packed(const MatvecProblem p, const PackedLayout L, const double* __restrict__ x, int64_t ldx,
                     double* __restrict__ y, int64_t ldy, int* __restrict__ err,
                     const uint64_t* __restrict__ binom) {
@@ -713,19 +803,20 @@ __global__ void __launch_bounds__(320, 2)
   const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t row = warp_id; row < p.n_rows; row += n_warps)
-    packed_row<GPL, INV, CPLX, K, FERMI>(T, p.group.n_bits, p.index, T.ch, p.group.spin_inversion, p.constraint, x, ldx,
-                                  y, ldy, row, err, binom, p.nnz_counter, p.real_elements != 0,
-                                  p.xs, p.ldxs);
+    packed_row<GPL, INV, CPLX, K, FERMI, PAIR>(T, p.group.n_bits, p.index, T.ch, p.group.spin_inversion, p.constraint,
+                                               x, ldx, y, ldy, row, err, binom, p.nnz_counter,
+                                               p.real_elements != 0, p.xs, p.ldxs);
 }
 
 // Batched kernel: the rows of all sectors form one row space that a persistent grid walks; each
 // warp looks up the sector of its row in the shared sector table.  `p` carries the shared
 // tables (site images, terms, constraint) of the first sector.
-template <int GPL, bool INV, int K>
-__global__ void __launch_bounds__(320, 2)
+template <int GPL, bool INV, int K, bool PAIR = false>
+__global__ void __launch_bounds__(320, (PAIR && GPL <= 2) ? 3 : 2)
     k_matvec_sectors(const MatvecProblem p, const PackedLayout L, const SectorDesc* __restrict__ sectors,
                      int n_sectors, int64_t total_rows, int64_t ldx, int64_t ldy, int* __restrict__ err,
-                     const uint64_t* __restrict__ binom) {
+                     const uint64_t* __restrict__ binom, const double* __restrict__ xs_all, int64_t ldxs,
+                     int col) {
   extern __shared__ __align__(16) unsigned char smem[];
   const PackedTables T = stage_packed(p, L, smem, false);
   SectorDesc* sd = (SectorDesc*)(smem + L.off_sectors);
@@ -749,8 +840,12 @@ __global__ void __launch_bounds__(320, 2)
       cur = lo;
     }
     const SectorDesc& S = sd[cur];
-    packed_row<GPL, INV, true, K>(T, p.group.n_bits, S.index, S.chars, (int)S.spin_inversion, p.constraint, S.x,
-                                  ldx, S.y, ldy, row - S.row_begin, err, binom, p.nnz_counter, S.real_elements != 0);
+    // gather source: the sector's rows of the prescaled copy of all columns (x_j * n_j, FP64 or
+    // pairs), if the launch made one
+    const double* xs = xs_all != nullptr ? xs_all + ((size_t)S.row_begin * ldxs + col) * 2 : nullptr;
+    packed_row<GPL, INV, true, K, false, PAIR>(T, p.group.n_bits, S.index, S.chars, (int)S.spin_inversion,
+                                               p.constraint, S.x, ldx, S.y, ldy, row - S.row_begin, err, binom,
+                                               p.nnz_counter, S.real_elements != 0, xs, ldxs);
   }
 }
 

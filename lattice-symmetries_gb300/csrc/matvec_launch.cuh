@@ -62,6 +62,31 @@ static int launch_with_smem(Kernel kern, const char* name, const MatvecProblem& 
     }                                                                                             \
   }
 
+// Defines NAME(gpl, inv, ...) launching the FP32-pair k_matvec_packed<GPL, INV, true, K, false, true>.
+#define LSG_DEFINE_PACKED_PAIR(NAME, K)                                                           \
+  int NAME(int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L, LaunchShape sh,      \
+           const double* x, int64_t ldx, double* y, int64_t ldy, int* err, const uint64_t* binom, \
+           cudaStream_t s) {                                                                      \
+    auto run = [&](auto gtag) -> int {                                                            \
+      constexpr int G = decltype(gtag)::value;                                                    \
+      return inv ? launch_with_smem(k_matvec_packed<G, true, true, K, false, true>, #NAME, p, L, sh, \
+                                    x, ldx, y, ldy, err, binom, s)                               \
+                 : launch_with_smem(k_matvec_packed<G, false, true, K, false, true>, #NAME, p, L,  \
+                                    sh, x, ldx, y, ldy, err, binom, s);                          \
+    };                                                                                            \
+    switch (gpl) {                                                                                \
+      case 1: return run(std::integral_constant<int, 1>{});                                       \
+      case 2: return run(std::integral_constant<int, 2>{});                                       \
+      case 3: return run(std::integral_constant<int, 3>{});                                       \
+      case 4: return run(std::integral_constant<int, 4>{});                                       \
+      case 6: return run(std::integral_constant<int, 6>{});                                       \
+      case 9: return run(std::integral_constant<int, 9>{});                                       \
+      case 12: return run(std::integral_constant<int, 12>{});                                     \
+      case 16: return run(std::integral_constant<int, 16>{});                                     \
+      default: return LS_GPU_ERR_INVALID;                                                         \
+    }                                                                                             \
+  }
+
 // Defines NAME(gpl, inv, ...) launching the fallback k_matvec_projected<GPL, INV, CPLX, 1>.
 #define LSG_DEFINE_FALLBACK(NAME, CPLX)                                                          \
   int NAME(int gpl, bool inv, const MatvecProblem& p, const SmemLayout& L, LaunchShape sh,       \

@@ -1,5 +1,6 @@
 // matvec_sectors.cu -- the batched (multi-sector) persistent matvec kernel: complex128,
-// K in {1, 4, 8, 16} right-hand sides, groups of up to 128 elements (GPL <= 4).
+// K in {1, 4, 8, 16} right-hand sides with FP64 accumulation, groups of up to 128 elements
+// (GPL <= 4).  The FP32-pair variants (K in {8, 16}) are in matvec_pairs_sec.cu.
 #include <type_traits>
 
 #include "matvec_launch.cuh"
@@ -8,10 +9,11 @@ namespace lsg {
 
 int launch_sectors(int k, int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L, LaunchShape sh,
                    const SectorDesc* d_desc, int n_sectors, int64_t total_rows, int64_t ldx, int64_t ldy,
-                   int* err, const uint64_t* binom, cudaStream_t s) {
+                   int* err, const uint64_t* binom, const double* xs_all, int64_t ldxs, int col, cudaStream_t s) {
   auto go = [&](auto kern) -> int {
     if (!ensure_smem_limit((const void*)kern, L.total)) return LS_GPU_ERR_CUDA;
-    kern<<<sh.blocks, sh.threads, L.total, s>>>(p, L, d_desc, n_sectors, total_rows, ldx, ldy, err, binom);
+    kern<<<sh.blocks, sh.threads, L.total, s>>>(p, L, d_desc, n_sectors, total_rows, ldx, ldy, err, binom, xs_all,
+                                                ldxs, col);
     return cuda_ok(cudaGetLastError(), "k_matvec_sectors") ? 0 : LS_GPU_ERR_CUDA;
   };
   auto with_k = [&](auto gtag, auto itag) -> int {

@@ -191,3 +191,24 @@ def test_first_matvec_on_a_fresh_basis_sees_its_norms():
         y = ls.Operator(b, expr).apply_device(torch.from_numpy(x).cuda()).cpu().numpy()
         yo = Case(b, expr).oracle_matvec(st, x, complex_=True, exact_norms=True)
         assert np.linalg.norm(y - yo) <= 1e-12 * np.linalg.norm(yo)
+
+
+def test_plan_forms_and_autotune():
+    """Both forms of a plan (one launch over all sectors, one launch per sector) give the same
+    result; the autotuner times both and keeps one; a plan that cannot batch refuses the form."""
+    import torch
+    ops = xxz_sector_ops(16)
+    batch = ls.SectorBatch(ops, k=16)
+    assert batch.batched
+    fill_random(batch, 21)
+    y1 = batch.run(check=True).clone()
+    batch.set_batched(False)
+    assert not batch.batched
+    y2 = batch.run(check=True).clone()
+    assert float((y1 - y2).abs().max()) <= 1e-14 * float(y1.abs().max())
+    t = batch.autotune()
+    assert t["ms_batched"] > 0 and t["ms_per_sector"] > 0
+    assert batch.batched == t["batched"]
+    y3 = batch.replay().clone()
+    torch.cuda.synchronize()
+    assert float((y3 - y1).abs().max()) <= 1e-14 * float(y1.abs().max())
