@@ -569,7 +569,7 @@ def run_sectors(args):
     torch.cuda.synchronize()
     t_fp64_block = start.elapsed_time(end) / 2
     y_fp64 = batch.Y.clone()
-    ls.Operator.block_arithmetic("pairs")
+    ls.Operator.block_arithmetic("auto")
     batch.run(check=True)
     pair_rel_l2 = float(torch.linalg.vector_norm(batch.Y - y_fp64) / torch.linalg.vector_norm(y_fp64))
     del y_fp64

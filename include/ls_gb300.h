@@ -408,14 +408,16 @@ int ls_gpu_enumerate_noalloc(ls_hs_basis const *basis, uint64_t *d_out, int64_t 
  * always runs 256-thread CTAs. */
 int ls_gpu_set_matvec_config(int threads_per_block, int waves);
 /* Arithmetic of complex blocks of 8 or 16 right-hand sides in the plain and the batched
- * multi-sector kernels: 1 (default) = FP32 pairs, 0 = FP64.  In the pair form x_j * n_j is stored once per
+ * multi-sector kernels: 0 = FP64; 1 (default) = FP32 pairs for groups of at most 64 elements,
+ * FP64 otherwise; 2 = FP32 pairs for every group.  In the pair form x_j * n_j is stored once per
  * call as two floats per component (16 bytes per complex element, like complex128), the
  * coefficient of each element is formed in FP64 and split, and the multiply-adds run on the
  * FP32 pipe with error-free products and two-sum accumulation (about 2^-46 relative per product;
- * H X agrees with the FP64 form to ~1e-14 relative).  With 16 columns the FP64 form is bound by
- * GB300's FP64 pipe (4 FP64 FMAs per element and column).  One right-hand side, real vectors
- * and blocks of 4 always run in FP64.  Returns LS_GPU_ERR_INVALID for other values. */
-int ls_gpu_set_block_arithmetic(int pairs);
+ * H X agrees with the FP64 form to ~1e-14 relative).  With a small group and 16 columns the FP64
+ * form is bound by GB300's FP64 pipe (4 FP64 FMAs per element and column); with a large group
+ * the integer orbit scan is the bound and FP64 is faster.  One right-hand side, real vectors and
+ * blocks of 4 always run in FP64.  Returns LS_GPU_ERR_INVALID for other values. */
+int ls_gpu_set_block_arithmetic(int mode);
 int ls_gpu_get_block_arithmetic(void);
 /* Most right-hand sides per kernel launch (16, 8, 4 or 1; larger k is split into launches). */
 int ls_gpu_set_matvec_rhs_tile(int rhs_tile);

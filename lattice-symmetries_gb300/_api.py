@@ -754,17 +754,23 @@ class Operator(_LinearOperator):
                 "autotune")
         return th.value, wv.value, ms.value
 
+    _ARITHMETIC = {"fp64": 0, "auto": 1, "pairs": 2}
+
     @staticmethod
     def block_arithmetic(mode: Optional[str] = None) -> str:
-        """Arithmetic of complex blocks of 8 or 16 right-hand sides: "pairs" (default: FP32-pair
-        multiply-adds from an FP64 coefficient and a prescaled pair copy of x, ~1e-14 relative to
-        the FP64 form) or "fp64".  Sets it when `mode` is given; returns the mode in force."""
+        """Arithmetic of complex blocks of 8 or 16 right-hand sides: "auto" (default: FP32-pair
+        multiply-adds from an FP64 coefficient and a prescaled pair copy of x for groups of at
+        most 64 elements, where FP64 bounds the kernel; ~1e-14 relative to the FP64 form),
+        "pairs" (pairs for every group) or "fp64".  Sets it when `mode` is given; returns the mode
+        in force."""
         lib = N.lib()
+        codes = Operator._ARITHMETIC
         if mode is not None:
-            if mode not in ("pairs", "fp64"):
-                raise ValueError("block arithmetic is 'pairs' or 'fp64'")
-            N.check(lib.ls_gpu_set_block_arithmetic(1 if mode == "pairs" else 0), "block arithmetic")
-        return "pairs" if lib.ls_gpu_get_block_arithmetic() == 1 else "fp64"
+            if mode not in codes:
+                raise ValueError("block arithmetic is 'auto', 'pairs' or 'fp64'")
+            N.check(lib.ls_gpu_set_block_arithmetic(codes[mode]), "block arithmetic")
+        cur = lib.ls_gpu_get_block_arithmetic()
+        return {v: k for k, v in codes.items()}[cur]
 
     @staticmethod
     def launch_config():

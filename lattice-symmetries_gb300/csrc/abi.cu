@@ -19,7 +19,7 @@ namespace lsg {
 int set_matvec_config(int threads, int blocks_per_sm);
 int set_matvec_rhs_tile(int tile);
 void get_matvec_config(int* threads, int* waves, int* rhs_tile);
-int set_block_arithmetic(int pairs);
+int set_block_arithmetic(int mode);
 int get_block_arithmetic();
 }
 
@@ -256,9 +256,10 @@ extern "C" int ls_gpu_set_matvec_rhs_tile(int rhs_tile) {
   return rc != 0 ? fail(rc, "the right-hand-side tile must be 1, 4, 8 or 16") : 0;
 }
 
-extern "C" int ls_gpu_set_block_arithmetic(int pairs) {
+extern "C" int ls_gpu_set_block_arithmetic(int mode) {
   std::lock_guard<std::mutex> lock(g_mutex);
-  if (set_block_arithmetic(pairs) != 0) return fail(LS_GPU_ERR_INVALID, "block arithmetic: 1 = FP32 pairs, 0 = FP64");
+  if (set_block_arithmetic(mode) != 0)
+    return fail(LS_GPU_ERR_INVALID, "block arithmetic: 0 = FP64, 1 = FP32 pairs for small groups, 2 = FP32 pairs");
   return 0;
 }
 

@@ -76,6 +76,8 @@ __global__ void __launch_bounds__(kThreads) k_block_gram(int64_t D, int k, int64
         mac(re, x.z, x.w, y.z, y.w);
         mac(im, x.x, x.y, y.z, y.w);
         mac(im, -x.z, -x.w, y.x, y.y);
+        renorm(re);
+        renorm(im);
       }
       dre += join(re);
       dim += join(im);
@@ -169,6 +171,8 @@ __global__ void __launch_bounds__(kThreads) k_block_update(int64_t D, int k, int
         mac(re, -x.z, -x.w, m.z, m.w);
         mac(im, x.x, x.y, m.z, m.w);
         mac(im, x.z, x.w, m.x, m.y);
+        renorm(re);
+        renorm(im);
       }
       if (two) {
         const float4* xq = x2s + rr * k;
@@ -179,6 +183,8 @@ __global__ void __launch_bounds__(kThreads) k_block_update(int64_t D, int k, int
           mac(re, -x.z, -x.w, m.z, m.w);
           mac(im, x.x, x.y, m.z, m.w);
           mac(im, x.z, x.w, m.x, m.y);
+          renorm(re);
+          renorm(im);
         }
       }
       out[at] = make_double2(join(re), join(im));

@@ -51,16 +51,21 @@ int set_matvec_rhs_tile(int tile) {
   return 0;
 }
 
-// Complex blocks of 8 or 16 right-hand sides accumulate in FP32 pairs (1) or in FP64 (0).
+// Complex blocks of 8 or 16 right-hand sides: 0 = FP64 multiply-adds; 1 = FP32 pairs where the
+// FP64 pipe bounds the kernel (groups of at most 64 elements: a short orbit scan per element
+// against 4 FP64 FMAs per element and column); 2 = FP32 pairs for every group.  With larger
+// groups the integer orbit scan is the bound and the pair form's extra instructions cost time.
 static int g_block_pairs = 1;
 
-int set_block_arithmetic(int pairs) {
-  if (pairs != 0 && pairs != 1) return LS_GPU_ERR_INVALID;
-  g_block_pairs = pairs;
+int set_block_arithmetic(int mode) {
+  if (mode < 0 || mode > 2) return LS_GPU_ERR_INVALID;
+  g_block_pairs = mode;
   return 0;
 }
 
 int get_block_arithmetic() { return g_block_pairs; }
+
+static bool use_pairs(int gpl) { return g_block_pairs == 2 || (g_block_pairs == 1 && gpl <= 2); }
 
 void get_matvec_config(int* threads, int* waves, int* rhs_tile) {
   if (threads) *threads = g_threads_override > 0 ? g_threads_override : 320;
@@ -138,7 +143,7 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
       // read no norm per generated element: FP64 for the FP64 kernels, float pairs for the pair
       // kernels.  Not when counting elements (the count needs the norms).
       const bool can_prescale = p.nnz_counter == nullptr && p.index.norms != nullptr;
-      const bool want_pairs = can_prescale && cplx && g_block_pairs != 0 &&
+      const bool want_pairs = can_prescale && cplx && use_pairs(p.group.gpl) &&
                               std::any_of(chunks.begin(), chunks.end(), [](int c) { return c >= 8; });
       const bool want_fp64 = can_prescale && std::any_of(chunks.begin(), chunks.end(), [&](int c) {
                                return !(want_pairs && c >= 8);
@@ -346,7 +351,7 @@ int sector_plan_run(const SectorPlan* plan, int* d_err, cudaStream_t s) {
   // chunks of 8 or 16 columns run the FP32-pair kernels from a prescaled pair copy of all
   // sectors' columns (one streaming pass); the others gather x and the norms in FP64
   float4* d_xp = nullptr;
-  const bool want_pairs = g_block_pairs != 0 && plan->shared.nnz_counter == nullptr &&
+  const bool want_pairs = use_pairs(plan->shared.group.gpl) && plan->shared.nnz_counter == nullptr &&
                           std::any_of(plan->chunks.begin(), plan->chunks.end(),
                                       [](const SectorPlan::Chunk& c) { return c.k >= 8; });
   if (want_pairs) {

@@ -645,6 +645,8 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
               mac(pre, -cih, -cil, xv[u].z, xv[u].w);
               mac(pim, cih, cil, xv[u].x, xv[u].y);
             }
+            renorm(pre);
+            renorm(pim);
           }
         }
       }

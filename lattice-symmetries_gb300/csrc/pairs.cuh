@@ -7,6 +7,8 @@
 //                 bits rounded to 24; integer instructions and one int->float conversion.
 //   mac           acc += a * b: hi*hi product made error-free with fmaf, first-order cross
 //                 terms, two-sum accumulation (about 2^-46 relative error per product).
+//   renorm        folds the low word back under ulp(hi) (after every few multiply-adds, so that
+//                 the low word's own rounding stays at 2^-48 of the running sum).
 //   join          (hi, lo) -> FP64 (exact conversions, one FP64 add).
 //
 // Range: magnitudes below 2^-126 split to 0; products above ~3e38 overflow to inf.
@@ -86,6 +88,14 @@ __device__ __forceinline__ F2 pair_add(F2 a, F2 b) {
 }
 
 __device__ __forceinline__ F2 pair_neg(F2 a) { return F2{-a.h, -a.l}; }
+
+// Moves the low word's accumulated value into the high word (fast two-sum, |h| >= |l|), so that
+// later additions to the low word round relative to ulp(h) again.
+__device__ __forceinline__ void renorm(F2& a) {
+  const float s = __fadd_rn(a.h, a.l);
+  a.l = __fsub_rn(a.l, __fsub_rn(s, a.h));
+  a.h = s;
+}
 
 // Warp butterfly step for a pair (both words exchanged).
 __device__ __forceinline__ F2 pair_shfl_xor(F2 a, int d) {

@@ -22,12 +22,13 @@ def rel_l2(a, b):
 
 @pytest.fixture
 def arithmetic():
-    """Restores the pair default after each test."""
+    """Restores the default ("auto") after each test."""
     yield ls.Operator.block_arithmetic
-    ls.Operator.block_arithmetic("pairs")
+    ls.Operator.block_arithmetic("auto")
 
 
 def both_modes(apply, arithmetic):
+    """(pairs for every group, FP64)."""
     arithmetic("fp64")
     y64 = apply()
     arithmetic("pairs")
@@ -128,12 +129,29 @@ def test_pair_batched_sectors_match_fp64(arithmetic):
 
 
 def test_block_arithmetic_setting(arithmetic):
-    assert arithmetic() == "pairs"
+    assert arithmetic() == "auto"
     assert arithmetic("fp64") == "fp64"
     assert arithmetic() == "fp64"
     with pytest.raises(ValueError):
         arithmetic("fp32")
     from importlib import import_module
     N = import_module("lattice-symmetries_gb300._native")
-    assert N.lib().ls_gpu_set_block_arithmetic(2) == -1
+    assert N.lib().ls_gpu_set_block_arithmetic(3) == -1
     assert arithmetic("pairs") == "pairs"
+    assert arithmetic("auto") == "auto"
+
+
+def test_auto_uses_pairs_for_small_groups_only(arithmetic):
+    """auto = pairs for a 16-element group (same result as "pairs"), FP64 for a 128-element group
+    (bit-identical to "fp64")."""
+    import torch
+    small = chain_case(16, k=8, p=1, inv=-1)
+    large = square_case(4, 2, 2, inv=1, J2=0.5)
+    for c, same_as in ((small, "pairs"), (large, "fp64")):
+        c.basis.build()
+        X = random_block(c.basis.number_states, 16, seed=9)
+        arithmetic("auto")
+        ya = c.op.apply_device(X)
+        arithmetic(same_as)
+        yb = c.op.apply_device(X)
+        assert torch.equal(ya, yb), same_as

@@ -175,3 +175,23 @@ def test_sector_lanczos_paired_equals_fp64():
         h = op.apply_device(torch.eye(d, dtype=torch.complex128, device="cuda")).cpu().numpy()
         ref = np.linalg.eigvalsh(h)[0]
         assert abs(e_pair[s] - ref) < 1e-10 * abs(ref), (s, e_pair[s], ref)
+
+
+def test_gram_and_update_on_blocks_larger_than_l2():
+    """4 sectors x 400,000 rows x 16 columns (410 MB per block): the Gram and a two-term update
+    against torch FP64 (this shape is also the one profiled for the dense kernels)."""
+    import torch
+    S, D, k = 4, 400000, 16
+    X = rand_block(S, D, k, seed=31)
+    Y = rand_block(S, D, k, seed=32)
+    G = gram(X, Y)
+    ref = X.mH @ Y
+    assert float(((G - ref).abs() / (X.abs().mT @ Y.abs())).max()) <= TOL
+    del ref
+    M1 = rand_block(S, k, k, seed=33)
+    M2 = rand_block(S, k, k, seed=34)
+    out = torch.empty_like(X)
+    update(out, 1.0, Y, X, M1, X, M2)
+    ref = Y + X @ (M1 + M2)
+    bound = Y.abs() + X.abs() @ (M1.abs() + M2.abs())
+    assert float(((out - ref).abs() / bound).max()) <= TOL
