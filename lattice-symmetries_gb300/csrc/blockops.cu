@@ -99,18 +99,34 @@ __global__ void __launch_bounds__(kThreads) k_block_gram(int64_t D, int k, int64
   }
 }
 
-__global__ void k_block_gram_sum(const double2* __restrict__ partial, int chunks, int nout, double2* __restrict__ G) {
+// G[s][o] = sum over chunks of partial[s][c][o]: block (s, o / 32), lane = o % 32; the 32 warps
+// of the block sum interleaved chunks, then lane o adds the 32 warp sums in order (fixed
+// summation order: deterministic).
+__global__ void __launch_bounds__(1024) k_block_gram_sum(const double2* __restrict__ partial, int chunks, int nout,
+                                                         double2* __restrict__ G) {
+  __shared__ double2 warp_sums[32][32];
   const int s = blockIdx.x;
-  const int o = threadIdx.x;
-  if (o >= nout) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int o = blockIdx.y * 32 + lane;
   double re = 0.0, im = 0.0;
-  const double2* p = partial + (size_t)s * chunks * nout + o;
-  for (int c = 0; c < chunks; ++c) {
-    const double2 v = p[(size_t)c * nout];
-    re += v.x;
-    im += v.y;
+  if (o < nout) {
+    const double2* p = partial + (size_t)s * chunks * nout + o;
+    for (int c = warp; c < chunks; c += 32) {
+      const double2 v = p[(size_t)c * nout];
+      re += v.x;
+      im += v.y;
+    }
   }
-  G[(size_t)s * nout + o] = make_double2(re, im);
+  warp_sums[warp][lane] = make_double2(re, im);
+  __syncthreads();
+  if (warp == 0 && o < nout) {
+    double2 t = make_double2(0.0, 0.0);
+    for (int w = 0; w < 32; ++w) {
+      t.x += warp_sums[w][lane].x;
+      t.y += warp_sums[w][lane].y;
+    }
+    G[(size_t)s * nout + o] = t;
+  }
 }
 
 // out[s, r, j] = beta W[s, r, j] + sum_i X1[s, r, i] M1[s, i, j] (+ X2 M2).  Thread t handles
@@ -229,7 +245,8 @@ int launch_block_gram(int64_t S, int64_t D, int k, const double* d_x, const doub
                                          reinterpret_cast<const double2*>(d_y), d_x == d_y, partial);
   bool ok = cuda_ok(cudaGetLastError(), "k_block_gram");
   if (ok) {
-    k_block_gram_sum<<<(unsigned)S, 256, 0, s>>>(partial, (int)chunks, nout, reinterpret_cast<double2*>(d_g));
+    k_block_gram_sum<<<dim3((unsigned)S, (unsigned)((nout + 31) / 32)), 1024, 0, s>>>(
+        partial, (int)chunks, nout, reinterpret_cast<double2*>(d_g));
     ok = cuda_ok(cudaGetLastError(), "k_block_gram_sum");
   }
   ok = cuda_ok(cudaFreeAsync(partial, s), "cudaFreeAsync(block Gram partials)") && ok;
