@@ -90,3 +90,27 @@ def test_lean_steps_reach_the_same_extremal_eigenvalues():
         W = torch.empty_like(Q)
         ev = lanczos.block_lanczos(lambda: W.copy_(H @ Q), Q, W, 14, lean=lean)
         assert float((ev[:, 0] - ref[:, 0]).abs().max()) < 1e-8
+
+
+def test_dense_mode_validation_and_update_forms():
+    """CPU tensors take the torch path in every mode; an unknown mode is an error; _update's
+    in-place and aliasing forms agree with the plain expression."""
+    g = torch.Generator().manual_seed(5)
+    S, D, k = 2, 30, 4
+    W = (torch.randn((S, D, k), generator=g, dtype=torch.float64) + 0j).to(torch.complex128)
+    X = torch.randn((S, D, k), generator=g, dtype=torch.complex128)
+    M = torch.randn((S, k, k), generator=g, dtype=torch.complex128)
+    with pytest.raises(ValueError):
+        lanczos._gram(W, W, dense="fp32")
+    for mode in (None, "paired", "fp64"):
+        assert torch.allclose(lanczos._gram(W, X, dense=mode), W.mH @ X)
+    ref = W + X @ M
+    out = W.clone()
+    lanczos._update(out, 1.0, out, X, M, dense="paired")
+    assert torch.allclose(out, ref)
+    out = X.clone()
+    lanczos._update(out, 0.0, None, out, M)  # out aliases X1
+    assert torch.allclose(out, X @ M)
+    out = torch.empty_like(W)
+    lanczos._update(out, -0.5, W, X, M, X, M)
+    assert torch.allclose(out, -0.5 * W + 2 * (X @ M))
