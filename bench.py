@@ -39,6 +39,8 @@ if REPO not in sys.path:
 NCU_CAPTURES = {
     "j1j2_6x6": {"traffic": 117.870e9 + 0.269e9, "alu_pipe_pct": 73.4,
                  "source": "profiles/k_matvec_packed_j1j2_6x6.md"},
+    "xxz24_sectors": {"traffic": 5.402e9 + 0.706e9, "alu_pipe_pct": 59.3, "fp64_pipe_pct": 20.9,
+                      "source": "profiles/k_matvec_sectors_pairs_xxz24.md"},
 }
 
 CONFIGS = {
@@ -642,7 +644,13 @@ def run_sectors(args):
                    "states": sum(sizes), "nnz": sum(nnzs), "rhs": k, "parallelism": "replicas",
                    "l2": "inputs larger than L2 (X, Y {:.2f} GB each)".format(batch.X.numel() * 16 / 1e9)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_source": peak_kind, "bytes_per_launch": bytes_per_launch},
+                     "traffic": NCU_CAPTURES.get(args.config, {}).get("traffic"),
+                     "alu_pipe_pct": NCU_CAPTURES.get(args.config, {}).get("alu_pipe_pct"),
+                     "fp64_pipe_pct": NCU_CAPTURES.get(args.config, {}).get("fp64_pipe_pct"),
+                     "peak_source": peak_kind, "bytes_per_launch": bytes_per_launch,
+                     "note": "issue-bound gather kernel (FP32-pair multiply-adds on small groups); frac is of "
+                             "algorithmic bytes with every gather counted from DRAM; traffic (ncu, batched "
+                             "launch) only for the workload captured whole"},
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_run * args.steps, "clocks": clocks.summary(),
         "basis_build_s": t_build,
         "extra": {"form": "one persistent launch over all sectors" if tune["batched"] else
