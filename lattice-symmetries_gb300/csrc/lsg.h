@@ -225,8 +225,8 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
 // Sector plans (matvec.cu): y_s = H_s x_s (complex, k right-hand sides, leading dimensions
 // ldx/ldy) for many sectors.  When the sectors share the group's site images, the terms and the
 // constraint (`shareable`), each RHS chunk is ONE persistent launch over all sectors' rows;
-// otherwise the plan launches the sectors one after the other.  Running a plan allocates nothing
-// and does not synchronise, so it can be captured in a CUDA graph.
+// otherwise the plan launches the sectors one after the other.  Running a plan allocates only
+// stream-ordered and does not synchronise, so it can be captured in a CUDA graph.
 struct SectorPlan;
 int sector_plan_build(const std::vector<MatvecProblem>& problems, bool shareable, int k,
                       const std::vector<const double*>& xs, int64_t ldx, const std::vector<double*>& ys,
