@@ -61,6 +61,27 @@ __device__ __forceinline__ int64_t mv_index_lookup(const DeviceIndex& ix, uint64
   return (base < ix.n_states && __ldg(ix.reps + base) == needle) ? base : -1;
 }
 
+// Re-reads an index descriptor that lives in shared memory (the batched kernel's sector table)
+// through volatile loads, so that the compiler reads it where the lookup needs it instead of
+// holding its fields in registers for the whole row.
+__device__ __forceinline__ DeviceIndex reload_index(const DeviceIndex* p) {
+  const volatile DeviceIndex* v = p;
+  DeviceIndex r;
+  r.n_states = v->n_states;
+  r.reps = v->reps;
+  r.norms = v->norms;
+  r.inv_norms = v->inv_norms;
+  r.offsets = v->offsets;
+  r.shift = v->shift;
+  r.range_size = v->range_size;
+  r.prefix_bits = v->prefix_bits;
+  r.max_state = v->max_state;
+  r.identity = v->identity;
+  r.combinadic = v->combinadic;
+  r.rank_base = v->rank_base;
+  return r;
+}
+
 struct C2 {
   double re, im;
 };
@@ -485,7 +506,7 @@ __device__ __forceinline__ PackedTables stage_packed(const MatvecProblem& p, con
 // (pairs.cuh): the coefficient is formed in FP64 and split once per element; each lane's pair
 // sums are converted to FP64 before the cross-lane reduction.  With 16 right-hand sides the FP64
 // form is bound by GB300's narrow FP64 pipe (4 FP64 FMAs per element and column).
-template <int GPL, bool INV, bool CPLX, int K, bool FERMI = false, bool PAIR = false>
+template <int GPL, bool INV, bool CPLX, int K, bool FERMI = false, bool PAIR = false, bool SMEM_IX = false>
 __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbits, const DeviceIndex& ix,
                                            const double2* __restrict__ chars, const int spin_inversion,
                                            const DeviceConstraint& cons, const double* __restrict__ x,
@@ -493,7 +514,9 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
                                            const int64_t row, int* __restrict__ err,
                                            const uint64_t* __restrict__ binom,
                                            unsigned long long* nnz_counter, const bool real_elements,
-                                           const double* __restrict__ xs = nullptr, const int64_t ldxs = 0) {
+                                           const double* __restrict__ xs = nullptr, const int64_t ldxs = 0,
+                                           const DeviceIndex* ix_smem = nullptr,
+                                           const double2* const* chars_smem = nullptr) {
   // gather source: x_j * n_j when prescaled (xs), else x_j with the norm applied per element
   const bool prescaled = xs != nullptr;
   const double* __restrict__ xg = prescaled ? xs : x;
@@ -590,9 +613,12 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
     if (lane < nslot) {
       const uint64_t rep = my_key >> SH;
       const uint32_t idx = (uint32_t)(my_key & lowmask);
-      j = mv_index_lookup(ix, rep, binom);
+      // SMEM_IX (batched kernel): the sector's index and characters are re-read from the shared
+      // sector table here, once per 32 elements
+      const DeviceIndex ixl = SMEM_IX ? reload_index(ix_smem) : ix;
+      j = mv_index_lookup(ixl, rep, binom);
       // a zero-norm column contributes nothing (prescaled: its x_j * n_j is already zero)
-      const double nj = prescaled ? 1.0 : (j >= 0 ? __ldg(ix.norms + j) : 0.0);
+      const double nj = prescaled ? 1.0 : (j >= 0 ? __ldg(ixl.norms + j) : 0.0);
       if (nj == 0.0) j = -1;
       found += (j >= 0);
       if (j >= 0) {
@@ -602,7 +628,9 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
         const long long sbit = (long long)(__popcll(beta & T.ts[my_t]) & 1) << 63;
         c.x = __longlong_as_double(__double_as_longlong(c.x) ^ sbit);
         c.y = __longlong_as_double(__double_as_longlong(c.y) ^ sbit);
-        double2 chi = chars[idx >> 1];
+        const double2* chs = chars;
+        if constexpr (SMEM_IX) chs = *(const double2* const volatile*)chars_smem;
+        double2 chi = chs[idx >> 1];
         if (INV && (idx & 1) && spin_inversion == -1) chi = make_double2(-chi.x, -chi.y);
         if constexpr (FERMI) {
           // g moves the fermions of beta onto the representative with the sign of the
@@ -845,9 +873,10 @@ __global__ void __launch_bounds__(320, (PAIR && GPL <= 2) ? 3 : 2)
     // gather source: the sector's rows of the prescaled copy of all columns (x_j * n_j, FP64 or
     // pairs), if the launch made one
     const double* xs = xs_all != nullptr ? xs_all + ((size_t)S.row_begin * ldxs + col) * 2 : nullptr;
-    packed_row<GPL, INV, true, K, false, PAIR>(T, p.group.n_bits, S.index, S.chars, (int)S.spin_inversion,
-                                               p.constraint, S.x, ldx, S.y, ldy, row - S.row_begin, err, binom,
-                                               p.nnz_counter, S.real_elements != 0, xs, ldxs);
+    packed_row<GPL, INV, true, K, false, PAIR, true>(T, p.group.n_bits, S.index, S.chars, (int)S.spin_inversion,
+                                                     p.constraint, S.x, ldx, S.y, ldy, row - S.row_begin, err,
+                                                     binom, p.nnz_counter, S.real_elements != 0, xs, ldxs,
+                                                     &S.index, &S.chars);
   }
 }
 
