@@ -412,7 +412,7 @@ int ls_gpu_set_matvec_config(int threads_per_block, int waves);
  * FP64 otherwise; 2 = FP32 pairs for every group.  In the pair form x_j * n_j is stored once per
  * call as two floats per component (16 bytes per complex element, like complex128), the
  * coefficient of each element is formed in FP64 and split, and the multiply-adds run on the
- * FP32 pipe with error-free products and two-sum accumulation (about 2^-46 relative per product;
+ * FP32 pipe with error-free products and two-sum accumulation (below 2^-45 relative per product;
  * H X agrees with the FP64 form to ~1e-14 relative).  With a small group and 16 columns the FP64
  * form is bound by GB300's FP64 pipe (4 FP64 FMAs per element and column); with a large group
  * the integer orbit scan is the bound and FP64 is faster.  One right-hand side, real vectors and
@@ -436,7 +436,7 @@ int ls_gpu_autotune_matvec(ls_hs_operator const *op, int k, int *best_threads, i
  *                        or X2 (each row is read before it is written).
  * The blocks stay FP64 in memory; the products are evaluated in FP32-pair arithmetic (each
  * FP64 input split into two floats, error-free hi*hi products, two-sum accumulation: about
- * 2^-46 relative per product, every entry within ~1e-14 of the sum of its terms' magnitudes)
+ * below 2^-45 relative per product, every entry within ~1e-13 of the sum of its terms' magnitudes)
  * because GB300's FP64 pipe is a small fraction of its FP32 rate.  Range: products of two
  * entries must stay below ~1e38 in magnitude (else inf), and lose low-order bits below ~1e-30
  * (orthonormal and H-applied blocks are far inside).

@@ -12,9 +12,9 @@
 // every FP64 input is split into an unevaluated sum hi + lo of two floats (48 significant bits;
 // the split uses integer instructions only), products are formed with an exact hi*hi term
 // (fmaf error term) plus the first-order cross terms, and running sums use an error-free
-// two-sum.  The relative error of one product is about 2^-46.  The Gram kernel keeps a pair sum
+// two-sum.  The relative error of one product is below 2^-45 (3e-14).  The Gram kernel keeps a pair sum
 // over one tile of 32 rows at a time and adds the tiles in FP64, so the error of a Gram entry
-// stays near 2^-46 of the sum of magnitudes of its terms.  Results are converted back to FP64
+// stays near that bound relative to the sum of magnitudes of its terms.  Results are converted back to FP64
 // (integer conversion + one FP64 add).
 //
 // Determinism: every CTA reduces a fixed row range; the partial Gram matrices are summed in

@@ -19,7 +19,7 @@ Ritz values can repeat ("ghosts"); the lowest ones are reliable.
 
 Dense products (`dense=`): "paired" (default on the GPU for k <= 16) runs the tall-skinny Gram
 matrices and block updates through the library's FP32-pair kernels (ls_gpu_block_gram /
-ls_gpu_block_update: FP64 storage, about 2^-44 relative error per product, several times the
+ls_gpu_block_update: FP64 storage, below 2^-45 relative error per product, several times the
 speed of FP64 GEMMs on GB300, whose FP64 pipe is narrow); "fp64" uses torch's FP64 GEMMs.
 CPU tensors always take the torch path.
 """

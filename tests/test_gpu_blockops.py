@@ -3,7 +3,7 @@ arithmetic) against torch FP64 on the same inputs, and block Lanczos with the FP
 against the same recurrence with torch FP64 GEMMs.
 
 Tolerance: every entry within 1e-13 of the sum of the magnitudes of its terms (one product is
-about 2^-46 relative; the Gram adds 32-row tiles in FP64)."""
+below 2^-45 relative; the Gram adds 32-row tiles in FP64)."""
 
 import importlib
 
