@@ -647,7 +647,7 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
       const F2 cr = split_double(fre), ci = split_double(fim);
       // U passes at a time: their gathers are issued before the multiply-adds, so that U loads
       // per lane are in flight (the pair arithmetic leaves the kernel latency-bound otherwise)
-      constexpr int U = 4;
+      constexpr int U = SMEM_IX ? 2 : 4;  // the batched kernel holds more live state per row
       const float4* __restrict__ xp = reinterpret_cast<const float4*>(xg);
       for (int s0 = 0; s0 < nslot; s0 += U * Q) {
         float4 xv[U];
