@@ -145,3 +145,26 @@ def test_operator_apply_to_basis_state_host_paths():
     assert len(out) == 1 and out[0] == (2 + 0j, 2)
     assert op.apply_diag_to_basis_state(1) == -1.0
     assert op.apply_diag_to_basis_state(3) == 1.0
+
+
+def test_host_side_settings_without_a_gpu():
+    """Settings that touch no device: block arithmetic modes, launch-shape validation, invalid
+    dense-product shapes and NULL plans are rejected with LS_GPU_ERR_INVALID and a message."""
+    lib = N.lib()
+    ls_ = __import__("importlib").import_module("lattice-symmetries_gb300")
+    assert ls_.Operator.block_arithmetic() == "auto"
+    for mode in ("fp64", "pairs", "auto"):
+        assert ls_.Operator.block_arithmetic(mode) == mode
+    assert lib.ls_gpu_set_block_arithmetic(-1) == -1
+    assert lib.ls_gpu_set_block_arithmetic(3) == -1
+    assert ls_.Operator.block_arithmetic() == "auto"
+    assert lib.ls_gpu_set_matvec_config(33, 0) == -1
+    assert lib.ls_gpu_set_matvec_config(352, 0) == -1
+    assert lib.ls_gpu_set_matvec_config(0, 65) == -1
+    assert lib.ls_gpu_block_gram(1, 10, 17, None, None, None, None) == -1
+    assert b"k <= 16" in lib.ls_gpu_last_error()
+    assert lib.ls_gpu_block_gram(0, 10, 4, None, None, None, None) == -1
+    assert lib.ls_gpu_block_update(1, 10, 4, 1.0, None, None, None, None, None, None, None) == -1
+    assert lib.ls_gpu_sector_plan_set_batched(None, 1) == -1
+    assert b"not a sector plan" in lib.ls_gpu_last_error()
+    N.take_errors()
