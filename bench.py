@@ -536,8 +536,10 @@ def run_sectors(args):
     # the plan's autotuner: one persistent launch over all sectors, or one launch per sector
     tune = batch.autotune()
     batch.capture()
-    # kernels per run: the prescaled pair copy of X + the matvec, once or per sector
-    launches_per_run = 2 if tune["batched"] else 2 * len(ops)
+    # kernels per run: batched, the prescaled pair copy of X (pair arithmetic; the n translations
+    # are at most 64 group elements) + the matvec; per sector, a prescaled copy + the matvec each
+    pairs_in_use = args.block_arithmetic == "pairs" or (args.block_arithmetic == "auto" and n <= 64)
+    launches_per_run = (1 + int(pairs_in_use)) if tune["batched"] else 2 * len(ops)
     stream = torch.cuda.current_stream()
     for _ in range(args.warmup):
         batch.replay()
@@ -571,7 +573,7 @@ def run_sectors(args):
     torch.cuda.synchronize()
     t_fp64_block = start.elapsed_time(end) / 2
     y_fp64 = batch.Y.clone()
-    ls.Operator.block_arithmetic("auto")
+    ls.Operator.block_arithmetic(args.block_arithmetic)
     batch.run(check=True)
     pair_rel_l2 = float(torch.linalg.vector_norm(batch.Y - y_fp64) / torch.linalg.vector_norm(y_fp64))
     del y_fp64
@@ -656,7 +658,7 @@ def run_sectors(args):
         "extra": {"form": "one persistent launch over all sectors" if tune["batched"] else
                   "one launch per sector (in the CUDA graph)",
                   "autotune_ms": {"batched": tune["ms_batched"], "per_sector": tune["ms_per_sector"]},
-                  "block_arithmetic": "FP32 pairs", "fp64_block_arithmetic_ms": t_fp64_block,
+                  "block_arithmetic": args.block_arithmetic, "fp64_block_arithmetic_ms": t_fp64_block,
                   "pairs_vs_fp64_rel_l2": pair_rel_l2,
                   "per_sector_launches_ms": t_loop, "batched_speedup_vs_per_sector": t_loop / t_ms,
                   "plain_one_vector_all_sectors_ms": t_plain,
@@ -729,11 +731,15 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the block-16 and adjoint lines")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--block-arithmetic", default="auto", choices=["auto", "pairs", "fp64"],
+                    help="multiply-adds of complex blocks of 8/16 columns (auto: FP32 pairs for groups of "
+                         "at most 64 elements)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    importlib.import_module("lattice-symmetries_gb300").Operator.block_arithmetic(args.block_arithmetic)
     if args.config in ("xxz24_sectors", "xxz28_sectors", "hubbard16", "ladder28_grad"):
         world, rank, _ = dist_setup()
         if rank != 0:
