@@ -168,3 +168,18 @@ def test_host_side_settings_without_a_gpu():
     assert lib.ls_gpu_sector_plan_set_batched(None, 1) == -1
     assert b"not a sector plan" in lib.ls_gpu_last_error()
     N.take_errors()
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    """Without the compiled library the binding raises instead of falling back to a CPU path."""
+    import subprocess
+    import sys
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    # the binding module alone (the package's __init__ would load the built library first)
+    code = ("import importlib.util as u; "
+            "s = u.spec_from_file_location('lsg_native', 'lattice-symmetries_gb300/_native.py'); "
+            "N = u.module_from_spec(s); s.loader.exec_module(N); "
+            "N.load({!r})".format(str(tmp_path / "absent" / "libls_gb300.so")))
+    res = subprocess.run([sys.executable, "-c", code], cwd=repo, capture_output=True, text=True)
+    assert res.returncode != 0
+    assert "ImportError" in res.stderr and "build_native.py" in res.stderr
