@@ -213,8 +213,10 @@ struct MatvecProblem {
   // Every off-diagonal matrix element is real (real term coefficients and real characters): a
   // complex right-hand side then needs 2 FP64 FMAs per element instead of 4.
   int real_elements = 0;
-  // Optional gather source x_j * n_j (x scaled by the orbit norms, leading dimension ldxs): the
-  // gathers then need no norm per element.  The diagonal still reads the caller's x.
+  // Optional gather source x_j * n_j (x scaled by the orbit norms, leading dimension ldxs in
+  // elements): the gathers then need no norm per element.  FP64 for the FP64 kernels; for the
+  // FP32-pair kernels each complex element is four floats [re_h, re_l, im_h, im_l] (the same 16
+  // bytes).  The diagonal still reads the caller's x.
   const double* xs = nullptr;
   int64_t ldxs = 0;
 };
