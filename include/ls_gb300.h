@@ -176,6 +176,24 @@ void ls_hs_internal_set_chpl_kernels(ls_chpl_kernels const *kernels);
  * CUDA stream / release device memory). */
 void ls_chpl_init(void);
 void ls_chpl_finalize(void);
+/* LatticeSymmetries.chpl:28-30 (declared at chapel/lib/lattice_symmetries_chapel.h:35):
+ * installs this library's drivers into the plugin table again (after a host replaced them). */
+void ls_chpl_init_kernels(void);
+/* Module initialisers of the Chapel library (chapel/lib/lattice_symmetries_chapel.h:5-42,
+ * called by chapel/src/library.c:23-31).  This library has no module state to initialise:
+ * chpl__init_LatticeSymmetries installs the drivers (the module body of LatticeSymmetries.chpl:32),
+ * the others do nothing.  The arguments (line and file of the call) are ignored.
+ * ls_hs_init / ls_hs_exit (types.h:61-62) start and stop the Haskell runtime; they belong to the
+ * Haskell host library and are not exported here. */
+void chpl__init_BatchedOperator(int64_t ln, int32_t fn);
+void chpl__init_CommonParameters(int64_t ln, int32_t fn);
+void chpl__init_ConcurrentAccessor(int64_t ln, int32_t fn);
+void chpl__init_DistributedMatrixVector(int64_t ln, int32_t fn);
+void chpl__init_FFI(int64_t ln, int32_t fn);
+void chpl__init_ForeignTypes(int64_t ln, int32_t fn);
+void chpl__init_LatticeSymmetries(int64_t ln, int32_t fn);
+void chpl__init_StatesEnumeration(int64_t ln, int32_t fn);
+void chpl__init_Vector(int64_t ln, int32_t fn);
 
 /* Orbit-scan kernel data: replaces ls_internal_create_halide_kernel_data (kernels.c:112-189,
  * bound at Basis.hs:915-919). Uploads masks, characters and the per-site image table of the
@@ -291,6 +309,11 @@ int ls_gpu_matvec_f64(ls_hs_operator const *op, int k, double const *d_x, int64_
 int ls_gpu_check_errors(void *stream);
 /* Number of off-diagonal matrix elements (generated targets found in the basis) of H. */
 int ls_gpu_count_nonzeros(ls_hs_operator const *op, int64_t *nnz);
+/* The kernel a matvec of `op` runs: *form = 2 for the packed projected kernel (its tables fit in
+ * shared memory; *slots_per_lane = group elements per lane, 32 lanes per warp), 1 for the
+ * fallback projected kernel (*slots_per_lane likewise), 0 for the thread-per-row kernel (no
+ * permutation group; *slots_per_lane = 0).  Needs a built basis. */
+int ls_gpu_matvec_kernel_info(ls_hs_operator const *op, int *form, int *slots_per_lane);
 
 /* Releases the device copies of an operator's term tables (made on the first GPU use of `op`,
  * keyed by its address).  Call before freeing or reusing the ls_hs_operator; no-op otherwise. */
@@ -397,8 +420,11 @@ int ls_gpu_state_index(ls_hs_basis const *basis, int64_t batch, uint64_t const *
  * first call on a device looks up that array's device address (cudaGetSymbolAddress); make the
  * first call before any stream capture.  Limits: group tables up to 1 MiB and about 5.2e9
  * candidate states (LS_GPU_ERR_INVALID beyond, with a message); LS_GPU_ERR_INVALID also when
- * *count exceeds `capacity` (nothing is written past d_out[capacity - 1]).  Calls share the
- * array, so calls that overlap on the GPU race; the call synchronises `stream` before returning. */
+ * *count exceeds `capacity` (nothing is written past d_out[capacity - 1]) and when d_out is NULL
+ * with a non-zero capacity.  This entry point does not set up the per-device runtime that the
+ * other entry points share (their stream, error word and tables are allocated on first use), so
+ * it may be the first call of the library on a device.  Calls share the array, so calls that
+ * overlap on the GPU race; the call synchronises `stream` before returning. */
 int ls_gpu_enumerate_noalloc(ls_hs_basis const *basis, uint64_t *d_out, int64_t capacity,
                              int64_t *count, void *stream);
 

@@ -14,7 +14,7 @@ several right-hand sides, adjoint), ``Basis.device_states`` / ``device_norms``.
 from __future__ import annotations
 
 import ctypes
-from ctypes import POINTER, byref, c_double, c_int64, c_uint8, c_uint64, c_void_p
+from ctypes import POINTER, byref, c_double, c_int, c_int64, c_uint8, c_uint64, c_void_p
 from typing import List, Optional, Sequence, Tuple, Union
 
 import numpy as np
@@ -784,6 +784,12 @@ class Operator(_LinearOperator):
         n = c_int64(0)
         N.check(self._lib.ls_gpu_count_nonzeros(self._payload, byref(n)), "count_nonzeros")
         return int(n.value)
+
+    def kernel_info(self):
+        """(form, slots_per_lane) of the matvec kernel: form "packed", "fallback" or "plain"."""
+        form, slots = c_int(0), c_int(0)
+        N.check(self._lib.ls_gpu_matvec_kernel_info(self._payload, byref(form), byref(slots)), "kernel_info")
+        return ("plain", "fallback", "packed")[form.value], int(slots.value)
 
 
 def load_library():

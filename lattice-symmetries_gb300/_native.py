@@ -182,6 +182,7 @@ _SIGNATURES = [
     ("ls_gpu_autotune_matvec", c_int, [POINTER(ls_hs_operator), c_int, POINTER(c_int), POINTER(c_int),
                                        POINTER(c_double)]),
     ("ls_gpu_count_nonzeros", c_int, [POINTER(ls_hs_operator), POINTER(c_int64)]),
+    ("ls_gpu_matvec_kernel_info", c_int, [POINTER(ls_hs_operator), POINTER(c_int), POINTER(c_int)]),
     ("ls_gpu_sector_plan_set_batched", c_int, [c_void_p, c_int]),
     ("ls_gpu_sector_plan_autotune", c_int, [c_void_p, c_void_p, POINTER(c_int), POINTER(c_double),
                                             POINTER(c_double)]),

@@ -226,6 +226,16 @@ static void install_gpu_drivers() {
 __attribute__((constructor)) static void lsg_on_load() { install_gpu_drivers(); }
 
 extern "C" void ls_chpl_init(void) { install_gpu_drivers(); }
+extern "C" void ls_chpl_init_kernels(void) { install_gpu_drivers(); }
+extern "C" void chpl__init_LatticeSymmetries(int64_t, int32_t) { install_gpu_drivers(); }
+extern "C" void chpl__init_BatchedOperator(int64_t, int32_t) {}
+extern "C" void chpl__init_CommonParameters(int64_t, int32_t) {}
+extern "C" void chpl__init_ConcurrentAccessor(int64_t, int32_t) {}
+extern "C" void chpl__init_DistributedMatrixVector(int64_t, int32_t) {}
+extern "C" void chpl__init_FFI(int64_t, int32_t) {}
+extern "C" void chpl__init_ForeignTypes(int64_t, int32_t) {}
+extern "C" void chpl__init_StatesEnumeration(int64_t, int32_t) {}
+extern "C" void chpl__init_Vector(int64_t, int32_t) {}
 extern "C" void ls_chpl_finalize(void) {
   std::lock_guard<std::mutex> lock(g_mutex);
   for (int d = 0; d < 16; ++d) {
@@ -1335,6 +1345,17 @@ extern "C" int ls_gpu_check_errors(void* stream) {
   std::lock_guard<std::mutex> lock(g_mutex);
   cudaStream_t s = (cudaStream_t)stream;  // NULL: the legacy default stream (CUDA convention)
   return read_and_clear_error(s);
+}
+
+extern "C" int ls_gpu_matvec_kernel_info(ls_hs_operator const* op, int* form, int* slots_per_lane) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (op == nullptr || form == nullptr || slots_per_lane == nullptr)
+    return fail(LS_GPU_ERR_INVALID, "operator and outputs must not be NULL");
+  MatvecProblem p;
+  const int rc = make_problem(op, false, &p);
+  if (rc != 0) return rc;
+  *form = matvec_kernel_form(p, slots_per_lane);
+  return 0;
 }
 
 extern "C" int ls_gpu_count_nonzeros(ls_hs_operator const* op, int64_t* nnz) {

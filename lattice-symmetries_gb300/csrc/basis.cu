@@ -1163,6 +1163,29 @@ static int noalloc_scratch_address(unsigned char** out) {
   return 0;
 }
 
+// SM count of the current device for the grid sizes of this path, read with
+// cudaDeviceGetAttribute and kept per device.  The library's shared runtime (stream, error word,
+// binomial table) is never touched here: setting it up allocates device memory.
+static int noalloc_sms() {
+  static int sms[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+  if (sms[dev] <= 0) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return 1;
+    sms[dev] = n;
+  }
+  return sms[dev];
+}
+
+static int noalloc_grid(int64_t n, int threads) {
+  int64_t blocks = (n + threads - 1) / threads;
+  const int64_t cap = (int64_t)noalloc_sms() * 32;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  return (int)blocks;
+}
+
 template <int DEPTH>
 __device__ inline uint32_t enum_tile_flags(const DeviceGroup& g, const EnumArgs& a, int64_t first, int* cnt) {
   uint32_t bits = 0;
@@ -1228,7 +1251,7 @@ template <int D>
 struct RunEnumerateNoalloc {
   static void run(const DeviceGroup& g, const EnumArgs& a, int32_t* counts, const int64_t* offsets,
                   uint64_t* out, int64_t capacity, int pass, cudaStream_t s) {
-    int64_t blocks = std::min<int64_t>(a.n_tiles, (int64_t)num_sms() * 8);
+    int64_t blocks = std::min<int64_t>(a.n_tiles, (int64_t)noalloc_sms() * 8);
     if (blocks < 1) blocks = 1;
     if (pass == 0)
       k_enumerate_count<D><<<(unsigned)blocks, kEnumThreads, 0, s>>>(g, a, counts);
@@ -1241,6 +1264,7 @@ int enumerate_states_noalloc(const OrbitData* od, const EnumerateRequest& req, u
                              int64_t capacity, int64_t* count, cudaStream_t s) {
   *count = 0;
   if (capacity < 0) return fail(LS_GPU_ERR_INVALID, "negative capacity");
+  if (d_out == nullptr && capacity > 0) return fail(LS_GPU_ERR_INVALID, "output buffer is NULL");
   if (ensure_binomials() != 0) return LS_GPU_ERR_CUDA;
   const int n_bits = (req.mode == 2 || req.mode == 3) ? 2 * req.number_sites : req.number_sites;
   if (req.lower > req.upper) return 0;
@@ -1280,9 +1304,9 @@ int enumerate_states_noalloc(const OrbitData* od, const EnumerateRequest& req, u
     if (n > capacity) return fail(LS_GPU_ERR_INVALID, "output capacity is smaller than the number of states");
     if (n == 0) return 0;
     if (req.mode == 1)
-      k_enumerate_plain<<<grid_for((n + 15) / 16, 256), 256, 0, s>>>(r0, n, h, n_bits, d_out);
+      k_enumerate_plain<<<noalloc_grid((n + 15) / 16, 256), 256, 0, s>>>(r0, n, h, n_bits, d_out);
     else
-      k_enumerate_spinful<<<grid_for(n / 16 + 1, 256), 256, 0, s>>>(rA, nA, hA, rB, nB, hB, ns, d_out);
+      k_enumerate_spinful<<<noalloc_grid(n / 16 + 1, 256), 256, 0, s>>>(rA, nA, hA, rB, nB, hB, ns, d_out);
     if (!cuda_ok(cudaGetLastError(), "enumerate (no allocation)")) return LS_GPU_ERR_CUDA;
     return cuda_ok(cudaStreamSynchronize(s), "enumerate (no allocation)") ? 0 : LS_GPU_ERR_CUDA;
   }

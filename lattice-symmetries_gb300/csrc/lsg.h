@@ -223,6 +223,8 @@ struct MatvecProblem {
 
 int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, int64_t ldx,
                   double* d_y, int64_t ldy, int* d_err, cudaStream_t s);
+// The kernel launch_matvec picks for p: 2 packed (*gpl slots per lane), 1 fallback, 0 plain.
+int matvec_kernel_form(const MatvecProblem& p, int* gpl);
 
 // Sector plans (matvec.cu): y_s = H_s x_s (complex, k right-hand sides, leading dimensions
 // ldx/ldy) for many sectors.  When the sectors share the group's site images, the terms and the

@@ -113,6 +113,20 @@ LaunchShape packed_shape(int64_t n_rows) {
   return LaunchShape{(int)blocks, threads};
 }
 
+// Which kernel launch_matvec runs for `p`: 2 packed projected (*gpl = slots per lane), 1 the
+// fallback projected kernel (*gpl = its slots per lane), 0 the thread-per-row kernel.
+int matvec_kernel_form(const MatvecProblem& p, int* gpl) {
+  *gpl = 0;
+  if (p.projection != 2) return 0;
+  const PackedLayout PL = make_packed_layout(p);
+  if (p.group.gpl > 0 && p.group.onehot_packed != nullptr && PL.total <= kMaxDynamicSmem) {
+    *gpl = p.group.gpl;
+    return 2;
+  }
+  *gpl = pick_gpl_for(p.group.n_elems);
+  return 1;
+}
+
 // Splits k right-hand sides into launches of 16, 8, 4 and 1 columns.
 int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, int64_t ldx,
                   double* d_y, int64_t ldy, int* d_err, cudaStream_t s) {

@@ -2,7 +2,8 @@
 
 Run in a container where the reference is present:
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    LS_REFERENCE_DIR=<reference source tree> python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --reference <reference source tree>
 
 Outputs (all committed, small):
   reference_goldens.json  known answers extracted from the reference's own tests and data:
@@ -13,6 +14,8 @@ Outputs (all committed, small):
       * lattice configs               chapel/data/heisenberg_chain_24_symm.yaml,
                                       chapel/data/heisenberg_square_6x6.yaml
       * C struct layouts              kernels/lattice_symmetries_types.h (compiled with gcc)
+      * declared functions            kernels/lattice_symmetries_types.h,
+                                      chapel/lib/lattice_symmetries_chapel.h
   reference_kernels.npz   outputs of the reference's own kernels/indexing.c and kernels/reference.c
                           (built by oracle/Makefile into oracle/_ref) on seeded inputs.
 """
@@ -355,13 +358,28 @@ def reference_kernel_outputs(ref, out_path):
     np.savez_compressed(out_path, **results)
 
 
+def declared_functions(ref):
+    """Names of the functions the reference's two C headers declare (a host linked against them
+    resolves these symbols)."""
+    out = {}
+    for rel in ("kernels/lattice_symmetries_types.h", "chapel/lib/lattice_symmetries_chapel.h"):
+        text = open(os.path.join(ref, rel), encoding="utf-8").read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        text = re.sub(r"#[^\n]*", "", text)
+        text = re.sub(r"typedef[^;]*;", "", text)
+        names = re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", text)
+        out[rel] = sorted({n for n in names if n.startswith(("ls_", "chpl__init_")) and not n.endswith("_type")})
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("LS_REFERENCE_DIR", "/root/reference"))
     args = ap.parse_args()
     ref = args.reference
-    if not os.path.isdir(ref):
-        sys.exit("reference tree not found at " + ref)
+    if not ref or not os.path.isdir(ref):
+        sys.exit("reference tree not found: pass --reference or set LS_REFERENCE_DIR")
     data = {
         "benes_kats": benes_kats(ref),
         "n10_chain": n10_chain(ref),
@@ -369,6 +387,7 @@ def main():
         "hphi": hphi(ref),
         "chapel_configs": chapel_configs(ref),
         "struct_layouts": struct_layouts(ref),
+        "declared_functions": declared_functions(ref),
     }
     with open(os.path.join(HERE, "reference_goldens.json"), "w", encoding="utf-8") as f:
         json.dump(data, f, ensure_ascii=False, indent=1)

@@ -21,7 +21,7 @@ def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     text = re.sub(r"typedef[^;]*;", "", text)
-    names = set(re.findall(r"\b(ls_[a-z0-9_]+)\s*\(", text))
+    names = set(re.findall(r"\b((?:ls|chpl__init)_[A-Za-z0-9_]+)\s*\(", text))
     return sorted(n for n in names if not n.endswith("_type"))
 
 
@@ -30,6 +30,44 @@ def test_every_declared_symbol_is_exported():
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
     assert missing == []
     assert len(declared_functions()) >= 40
+
+
+# Started and stopped by the Haskell host library, which stays the host (haskell/cbits/init.c).
+HASKELL_RUNTIME = {"ls_hs_init", "ls_hs_exit"}
+
+
+def test_reference_headers_resolve(goldens):
+    """A host linked against the reference's two C headers (kernels/lattice_symmetries_types.h,
+    chapel/lib/lattice_symmetries_chapel.h) finds every function it declares in libls_gb300.so,
+    apart from the Haskell runtime's start and stop."""
+    lib = ctypes.CDLL(N.LIB_PATH)
+    declared = goldens["declared_functions"]
+    assert set(declared) == {"kernels/lattice_symmetries_types.h", "chapel/lib/lattice_symmetries_chapel.h"}
+    names = sorted(set(sum(declared.values(), [])) - HASKELL_RUNTIME)
+    assert "ls_chpl_init_kernels" in names and len(names) >= 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert missing == []
+    ours = set(declared_functions())
+    assert [n for n in names if n not in ours] == []
+
+
+def test_init_kernels_reinstalls_the_drivers():
+    """ls_chpl_init_kernels (LatticeSymmetries.chpl:28-30) puts the library's drivers back into the
+    plugin table after a host replaced them; chpl__init_LatticeSymmetries does the same."""
+    lib = N.lib()
+    lib.ls_chpl_init_kernels.restype = None
+    lib.chpl__init_LatticeSymmetries.restype = None
+    lib.chpl__init_LatticeSymmetries.argtypes = [ctypes.c_int64, ctypes.c_int32]
+    empty = N.ls_chpl_kernels()
+    for reinstall in (lambda: lib.ls_chpl_init_kernels(), lambda: lib.chpl__init_LatticeSymmetries(1, 2)):
+        lib.ls_hs_internal_set_chpl_kernels(ctypes.byref(empty))
+        assert lib.ls_hs_internal_get_chpl_kernels().contents.matrix_vector_product is None
+        reinstall()
+        k = lib.ls_hs_internal_get_chpl_kernels().contents
+        assert k.enumerate_states == N.fn_address("ls_chpl_enumerate_representatives")
+        assert k.operator_apply_off_diag == N.fn_address("ls_chpl_operator_apply_off_diag")
+        assert k.operator_apply_diag == N.fn_address("ls_chpl_operator_apply_diag")
+        assert k.matrix_vector_product == N.fn_address("ls_chpl_matrix_vector_product")
 
 
 def test_struct_layouts_match_reference(goldens):
@@ -167,6 +205,12 @@ def test_host_side_settings_without_a_gpu():
     assert lib.ls_gpu_block_update(1, 10, 4, 1.0, None, None, None, None, None, None, None) == -1
     assert lib.ls_gpu_sector_plan_set_batched(None, 1) == -1
     assert b"not a sector plan" in lib.ls_gpu_last_error()
+    # the allocation-free enumeration rejects a NULL output with a non-zero capacity before it
+    # touches the device
+    basis = ls_.SpinBasis(8, 4)
+    count = ctypes.c_int64(-1)
+    assert lib.ls_gpu_enumerate_noalloc(basis._payload, None, 70, ctypes.byref(count), None) == -1
+    assert b"NULL" in lib.ls_gpu_last_error()
     N.take_errors()
 
 
