@@ -10,11 +10,14 @@ A step is one plain single-vector H*x (complex128) over the whole sector.
     metric  = matrix elements / s = (D + NNZ) / t     (NNZ: off-diagonal elements of H)
     value   = device-resident x, CUDA events around K steps on the launching stream
     e2e     = the same metric through the reference-facing C-ABI call ls_chpl_matrix_vector_product
-              with host buffers (a complex x is two real calls), copies inside the timed region
+              with host buffers (one call with num_vectors = 2: Re x and Im x, which the real
+              Hamiltonian of this sector maps separately), copies inside the timed region
     extra   = block H*X with 16 right-hand sides and the adjoint H^dagger x, per vector
 
 `--impl reference` times the CPU restatement of the reference's algorithm (Benes orbit scan,
-scatter with atomics, prefix-table index; oracle/ls_oracle.c) with all host threads.
+scatter with atomics, prefix-table index; oracle/ls_oracle.c) with all host threads, on seeded
+random column samples of a basis that the restatement enumerates itself (the setup, also
+reported); it loads nothing of the product (oracle/workloads.py restates the workload).
 """
 
 from __future__ import annotations
@@ -150,49 +153,131 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_port_timing(basis, op, x, budget_s, threads):
-    """Times the oracle's reference-algorithm port on a bounded sample of columns.
-
-    Returns (elements_per_s, sample_description)."""
+def _oracle():
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
 
     O.build()
-    O.set_threads(threads)
-    states = np.asarray(basis.states)
-    D = len(states)
-    if basis.has_permutation_symmetries:
-        gens = [(s.permutation, s.sector) for s in basis.symmetries.generators]
-        el = O.close_group(gens)
-        re, im = O.characters(el)
-        masks, shifts = basis.symmetries.network()
-        g = O.Group(np.array([e[0] for e in el]), re, im, basis._c.spin_inversion, basis.number_bits, masks, shifts)
-        projection = 2
-        import torch
-        norms = torch.as_tensor(basis.device_norms(), device="cuda").cpu().numpy() if D > 0 else np.ones(0)
-    else:
-        g, projection, norms = None, (1 if basis._c.spin_inversion else 0), np.ones(D)
-    off = O.Terms(*op._off_arrays)
-    diag = O.Terms(*op._diag_arrays)
-    xc = np.asarray(x)
+    return O
 
-    def run(cols):
+
+def random_columns(rng, D, n):
+    """A seeded random sample of about n distinct column indices of [0, D), sorted."""
+    n = int(min(n, D))
+    if n >= D // 2:
+        return np.sort(rng.choice(D, size=n, replace=False)).astype(np.int64)
+    return np.unique(rng.integers(0, D, size=n)).astype(np.int64)
+
+
+class ColumnSampler:
+    """The CPU restatement of the reference's matvec (oracle/ls_oracle.c lso_matvec_sample: Benes
+    orbit scan in the reference's chunk order, prefix-table index of kernels/indexing.c, scatter
+    with relaxed atomic adds as DistributedMatrixVector.chpl:91-143) over seeded random samples of
+    columns, on `threads` host threads.  A step processes one sample: the orbit norms of its
+    column states (state_info, as BatchedOperator.chpl:232-238 does per batch) and the scatter."""
+
+    def __init__(self, O, group, inv, nbits, reps, off, diag, x, threads, seed):
+        self.O = O
+        O.set_threads(threads)
+        self.group, self.inv, self.nbits = group, inv, nbits
+        self.reps = np.ascontiguousarray(reps, dtype=np.uint64)
+        self.D = len(self.reps)
+        self.off, self.diag = off, diag
+        self.x = np.ascontiguousarray(x, dtype=np.complex128)
+        self.index = O.Index(self.reps, nbits, 22)
+        self.y = np.zeros(self.D, dtype=np.complex128)
+        self.rng = np.random.default_rng(seed)
+        self.threads = threads
+
+    def run(self, cols):
         t0 = time.perf_counter()
-        _, st, nnz = O.matvec(g, projection, basis._c.spin_inversion, basis.number_bits, states, norms, off, diag,
-                              xc, complex_=np.iscomplexobj(xc), baseline=True, cols=(0, cols), return_nnz=True)
+        norms = self.O.state_info(self.group, self.reps[cols], lane_width=8, use_benes=True)[2]
+        nnz = self.O.matvec_sample(self.group, 2, self.inv, self.nbits, self.reps, cols, norms, self.off, self.diag,
+                                   self.x[cols], self.y, self.index)
         return time.perf_counter() - t0, nnz
 
-    n = min(D, 512)
-    t, _ = run(n)
-    while t < 1.0 and n < D:
-        n = min(D, n * 4)
-        t, _ = run(n)
-    per_col = t / n
-    cols = int(min(D, max(n, budget_s / max(per_col, 1e-12))))
-    t, nnz = run(cols)
-    # matrix elements processed by the sample: its diagonal entries plus the off-diagonal
-    # elements its columns generated
-    return cols, nnz, t
+    def calibrate(self, seconds):
+        """Columns per sample so that one sample takes about `seconds`."""
+        n = 256
+        while True:
+            t, _ = self.run(random_columns(self.rng, self.D, n))
+            if t >= 0.25 or n >= self.D:
+                break
+            n = min(self.D, n * 4)
+        return int(min(self.D, max(n, seconds / max(t / n, 1e-12))))
+
+    def timed(self, n_cols, warmup, steps):
+        """Elements per second over `steps` fresh samples (after `warmup` untimed ones):
+        (sampled columns + their off-diagonal elements) / time."""
+        for _ in range(warmup):
+            self.run(random_columns(self.rng, self.D, n_cols))
+        tot_t, tot_e, cols_done = 0.0, 0, 0
+        for _ in range(steps):
+            cols = random_columns(self.rng, self.D, n_cols)
+            t, nnz = self.run(cols)
+            tot_t += t
+            tot_e += len(cols) + nnz
+            cols_done += len(cols)
+        return tot_e / tot_t, tot_t / steps, cols_done // max(1, steps)
+
+    def column_products(self, cols, coef):
+        """y = H[:, cols] coef (the oracle's scatter of those columns alone)."""
+        self.y[:] = 0
+        norms = self.O.state_info(self.group, self.reps[cols], lane_width=8, use_benes=True)[2]
+        self.O.matvec_sample(self.group, 2, self.inv, self.nbits, self.reps, cols, norms, self.off, self.diag, coef,
+                             self.y, self.index)
+        return self.y.copy()
+
+
+def oracle_inputs(O, basis, op):
+    """The oracle's group and term tables for a product basis and operator (our arm's CPU leg)."""
+    gens = [(sym.permutation, sym.sector) for sym in basis.symmetries.generators]
+    el = O.close_group(gens)
+    re, im = O.characters(el)
+    masks, shifts = basis.symmetries.network()
+    g = O.Group(np.array([e[0] for e in el]), re, im, basis._c.spin_inversion, basis.number_bits, masks, shifts)
+    return g, O.Terms(*op._off_arrays), O.Terms(*op._diag_arrays)
+
+
+def bench_config(name, D):
+    """The `config` object of both arms (identical for the same workload)."""
+    return {"workload": name, "description": CONFIGS[name]["description"], "number_states": D, "rhs": 1,
+            "parallelism": "replicas",
+            "l2": "inputs larger than L2 (x 16 B/state, representatives + norms + index)"}
+
+
+def enumeration_pin(name):
+    path = os.path.join(REPO, "tests", "golden", "enumeration_pins.json")
+    key = {"j1j2_6x6": "square6_pipi_z1"}.get(name)
+    if key is None or not os.path.exists(path):
+        return None
+    with open(path) as f:
+        return json.load(f).get(key)
+
+
+def check_parity(sampler, op, D, x_host, name, states):
+    """The GPU's H x_s against the oracle's scatter of the same sampled columns (x_s = x on 64
+    seeded random columns, zero elsewhere), outside every timed region; plus the enumeration
+    against the oracle's full-sector pin where one exists."""
+    import hashlib
+
+    import torch
+    cols = random_columns(np.random.default_rng(11), D, 64)
+    y_ref = sampler.column_products(cols, x_host[cols])
+    xs = torch.zeros(D, dtype=torch.complex128, device="cuda")
+    xs[torch.from_numpy(cols).cuda()] = torch.from_numpy(np.ascontiguousarray(x_host[cols])).cuda()
+    y = op.apply_device(xs).cpu().numpy()
+    tol = 1e-12 * np.abs(y_ref).max()
+    rows_equal = bool(np.array_equal(np.nonzero(np.abs(y) > tol)[0], np.nonzero(np.abs(y_ref) > tol)[0]))
+    out = {"columns": int(len(cols)), "rel_l2": float(np.linalg.norm(y - y_ref) / np.linalg.norm(y_ref)),
+           "nonzero_rows_equal": rows_equal, "tolerance": 1e-12,
+           "oracle": "oracle/ls_oracle.c lso_matvec_sample (scatter of the same columns)"}
+    pin = enumeration_pin(name)
+    if pin is not None:
+        out["enumeration_matches_oracle_pin"] = bool(
+            len(states) == pin["count"] and
+            hashlib.sha256(np.ascontiguousarray(states).astype("<u8").tobytes()).hexdigest() == pin["sha256"])
+    return out
 
 
 # ------------------------------------------------------------------------------------------------
@@ -212,75 +297,51 @@ def _cuda_available() -> bool:
 
 
 def run_reference(args):
-    """--impl reference: the CPU restatement of the reference's algorithm on the host cores."""
+    """--impl reference: the CPU restatement of the reference's algorithm on the host cores, built
+    from the oracle alone (oracle/workloads.py); nothing of the product is loaded."""
+    import hashlib
+
     world, rank, local = dist_setup()
     if rank != 0:
         return 0
+    if args.config not in ("j1j2_6x6", "chain24"):
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm covers the single-sector "
+                          "workloads j1j2_6x6 and chain24; run it with one of them"}))
+        return 0
+    O = _oracle()
     sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import oracle as O
+    import workloads as WL
 
-    O.build()
     threads = os.cpu_count() or 1
     O.set_threads(threads)
-    ls = importlib.import_module("lattice-symmetries_gb300")
-    lat = importlib.import_module("lattice-symmetries_gb300.lattices")
-    basis, expr = build_workload(ls, lat, args.config)
-    op = ls.Operator(basis, expr)
-    gens = [(s.permutation, s.sector) for s in basis.symmetries.generators]
-    el = O.close_group(gens)
-    re, im = O.characters(el)
-    masks, shifts = basis.symmetries.network()
-    inv = basis._c.spin_inversion
-    g = O.Group(np.array([e[0] for e in el]), re, im, inv, basis.number_bits, masks, shifts)
-    # Setup (untimed): the representatives come from the library's GPU enumeration; enumerating
-    # the 6x6 sector's 4.5e9 candidates on the host cores takes hours (0.1 % of the range did not
-    # finish in 10 minutes on 8 cores).  The timed steps below are the CPU restatement only.
+    w = WL.workload(args.config)
+    lo, hi = w.estimates()
+    # Setup (untimed for the matvec metric, reported on its own): the reference's enumeration,
+    # StatesEnumeration.chpl:242-268, over every candidate of the sector on all host threads.
     t0 = time.perf_counter()
-    if _cuda_available():
-        basis.build()
-        states = np.asarray(basis.states).copy()
-        setup = "representatives from the GPU enumeration"
-    else:
-        lo, hi = basis._estimates()
-        states = O.enumerate_projected(g, lo, hi, use_benes=True)
-        setup = "representatives from the host enumeration"
-    t_build = time.perf_counter() - t0
-    D = len(states)
-    norms = O.state_info(g, states, use_benes=True)[2]
+    reps = O.enumerate_projected_par(w.group, lo, hi, lane_width=8, use_benes=True)
+    t_enum = time.perf_counter() - t0
+    candidates = O.rank(hi) - O.rank(lo) + 1
+    D = len(reps)
     rng = np.random.default_rng(CONFIGS[args.config]["seed"])
     x = rng.normal(size=D) + 1j * rng.normal(size=D)
-    off = O.Terms(*op._off_arrays)
-    diag = O.Terms(*op._diag_arrays)
-    # calibrate columns per step for ~args.cpu_seconds / (steps + warmup) of work
-    per_step = max(1.0, args.cpu_seconds / max(1, args.steps + args.warmup))
-
-    def run(cols):
-        t = time.perf_counter()
-        _, _, nnz = O.matvec(g, 2, inv, basis.number_bits, states, norms, off, diag, x, complex_=True,
-                             baseline=True, cols=(0, cols), return_nnz=True)
-        return time.perf_counter() - t, nnz
-
-    n = min(D, 256)
-    t, _ = run(n)
-    while t < 0.5 and n < D:
-        n = min(D, n * 4)
-        t, _ = run(n)
-    cols = int(min(D, max(n, per_step / max(t / n, 1e-12))))
-    for _ in range(args.warmup):
-        run(cols)
-    runs = [run(cols) for _ in range(args.steps)]
-    tm = float(np.mean([r[0] for r in runs]))
-    nnz_sample = runs[0][1]
-    value = (cols + nnz_sample) / tm
+    sampler = ColumnSampler(O, w.group, w.inv, w.n, reps, w.off, w.diag, x, threads, seed=7)
+    per_step = max(0.2, args.cpu_seconds / max(1, args.steps + args.warmup))
+    n_cols = sampler.calibrate(per_step)
+    value, t_step, cols = sampler.timed(n_cols, args.warmup, args.steps)
     line = {
         "impl": "reference", "metric": "H*x matrix elements/s", "value": value, "unit": "elements/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": tm * 1e3,
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-        "data": "synthetic", "config": {"workload": args.config, "number_states": D},
+        "data": "synthetic", "config": bench_config(args.config, D),
         "cpu_baseline": {"value": value, "unit": "elements/s", "cores": threads, "kind": "port",
-                         "sample": "first {} of {} columns per step (scatter form, oracle/ls_oracle.c); setup: {} ({:.1f} s)".format(
-                             cols, D, setup, t_build)},
+                         "sample": "per step a fresh seeded random sample of {} of {} columns (oracle/ls_oracle.c "
+                                   "lso_matvec_sample: Benes orbit scan, prefix index, atomic scatter); basis from the "
+                                   "oracle's own enumeration".format(cols, D)},
         "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "enumeration": {"candidates": candidates, "states": D, "seconds": t_enum,
+                        "candidates_per_s": candidates / t_enum, "cores": threads,
+                        "sha256": hashlib.sha256(reps.astype("<u8").tobytes()).hexdigest()},
     }
     print(json.dumps(line))
     return 0
@@ -633,11 +694,16 @@ def run_sectors(args):
     cpu = None
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        x0 = batch.x(0)[:, 0].cpu().numpy()
-        cols, nnz_cols, tc = cpu_port_timing(ops[0].basis, ops[0], x0, args.cpu_seconds, threads)
-        cpu = {"value": (cols + nnz_cols) / tc, "unit": "elements/s", "cores": threads, "kind": "port",
-               "sample": "sector k=0 z=+1, first {} of {} columns, one vector (oracle/ls_oracle.c), {:.1f} s".format(
-                   cols, sizes[0], tc)}
+        O = _oracle()
+        b0 = ops[0].basis
+        g0, off0, diag0 = oracle_inputs(O, b0, ops[0])
+        sampler = ColumnSampler(O, g0, b0._c.spin_inversion, b0.number_bits, b0.states, off0, diag0,
+                                batch.x(0)[:, 0].cpu().numpy(), threads, seed=7)
+        n_cols = sampler.calibrate(args.cpu_seconds / 4)
+        rate, t_s, cols = sampler.timed(n_cols, 1, 3)
+        cpu = {"value": rate, "unit": "elements/s", "cores": threads, "kind": "port",
+               "sample": "sector k=0 z=+1, one vector, 3 seeded random samples of {} of {} columns "
+                         "(oracle/ls_oracle.c lso_matvec_sample), {:.2f} s each".format(cols, sizes[0], t_s)}
     line = {
         "metric": "H*x matrix elements/s", "value": value, "unit": "elements/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms, "higher_is_better": True,
@@ -829,30 +895,39 @@ def main():
                "path": "ls_chpl_matrix_vector_product(num_vectors=2: Re x, Im x), host buffers",
                "two_single_vector_calls": {"value": world * elements / t_two}}
 
-    cpu = None
+    cpu, parity = None, None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        cols, nnz_cols, tc = cpu_port_timing(basis, op, x_host, args.cpu_seconds, threads)
-        cpu = {"value": (cols + nnz_cols) / tc, "unit": "elements/s", "cores": threads, "kind": "port",
-               "sample": "first {} of {} columns, scatter form (oracle/ls_oracle.c, Benes + atomics), {:.1f} s".format(
-                   cols, D, tc)}
+        O = _oracle()
+        g, off, diag = oracle_inputs(O, basis, op)
+        states = basis.states
+        sampler = ColumnSampler(O, g, basis._c.spin_inversion, basis.number_bits, states, off, diag, x_host,
+                                threads, seed=7)
+        per_step = max(0.2, args.cpu_seconds / 6)
+        n_cols = sampler.calibrate(per_step)
+        rate, t_s, cols = sampler.timed(n_cols, 1, 5)
+        cpu = {"value": rate, "unit": "elements/s", "cores": threads, "kind": "port",
+               "sample": "5 seeded random samples of {} of {} columns (oracle/ls_oracle.c lso_matvec_sample: "
+                         "Benes orbit scan, prefix index, atomic scatter), {:.2f} s each".format(cols, D, t_s)}
+        parity = check_parity(sampler, op, D, x_host, args.config, states)
 
     if rank == 0:
         line = {
             "metric": "H*x matrix elements/s", "value": value, "unit": "elements/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": args.config, "description": CONFIGS[args.config]["description"],
-                       "number_states": D, "nnz": nnz, "rhs": 1, "parallelism": "replicas",
-                       "l2": "inputs larger than L2 (x 16 B/state, representatives + norms + index)"},
+            "config": bench_config(args.config, D),
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",
                          "frac": achieved_gbs / peak, "peak_source": peak_kind,
                          "traffic": NCU_CAPTURES.get(args.config, {}).get("traffic"),
                          "alu_pipe_pct": NCU_CAPTURES.get(args.config, {}).get("alu_pipe_pct"),
+                         "traffic_source": NCU_CAPTURES.get(args.config, {}).get("source"),
                          "bytes_per_launch": bytes_per_launch,
-                         "note": "integer-ALU bound orbit scan (alu_pipe_pct from ncu); frac is of algorithmic "
-                                 "bytes, traffic is ncu DRAM bytes per launch"},
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 2 * args.steps,
+                         "note": "integer-ALU bound orbit scan; frac is of algorithmic bytes; traffic (DRAM bytes "
+                                 "per launch) and alu_pipe_pct are from the ncu capture named in traffic_source, "
+                                 "not measured by this run"},
+            "nnz": nnz,
+            "cpu_baseline": cpu, "parity": parity, "e2e": e2e, "gpu_launches": 2 * args.steps,
             "clocks": clocks.summary(), "basis_build_s": t_build, "extra": extra,
             "autotune": {"threads": tuned[0], "waves": tuned[1], "ms": tuned[2]},
         }

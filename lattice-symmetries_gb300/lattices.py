@@ -57,6 +57,67 @@ def square_symmetries(L: int, kx: int = 0, ky: int = 0, point_group: bool = True
     return [Symmetry(tx, kx), Symmetry(ty, ky), Symmetry(rx, 0), Symmetry(ry, 0), Symmetry(rot, 0)]
 
 
+def triangular_index(x: int, y: int, L: int) -> int:
+    """Site x * a1 + y * a2 of an L x L triangular torus (a1 = (1, 0), a2 = (1/2, sqrt(3)/2))."""
+    return (y % L) * L + (x % L)
+
+
+def triangular_bonds(L: int) -> List[Tuple[int, int]]:
+    """Nearest-neighbour bonds of an L x L triangular torus (directions a1, a2, a2 - a1)."""
+    out = []
+    for y in range(L):
+        for x in range(L):
+            i = triangular_index(x, y, L)
+            out.append((i, triangular_index(x + 1, y, L)))
+            out.append((i, triangular_index(x, y + 1, L)))
+            out.append((i, triangular_index(x - 1, y + 1, L)))
+    return out
+
+
+def triangular_symmetries(L: int, k1: int = 0, k2: int = 0, rotation: int = 0, reflection: int = None
+                          ) -> List[Symmetry]:
+    """Translations (sectors k1, k2), the 60-degree rotation (x, y) -> (-y, x + y) with sector
+    `rotation` (of 6) and, unless reflection is None, the mirror (x, y) -> (y, x) with that sector:
+    the group T x C6 (6 L^2 elements) or T x C6v (12 L^2).  As on the square torus, the point group
+    only combines with momenta it maps to themselves."""
+    n = L * L
+    t1 = [triangular_index(i % L + 1, i // L, L) for i in range(n)]
+    t2 = [triangular_index(i % L, i // L + 1, L) for i in range(n)]
+    rot = [triangular_index(-(i // L), i % L + i // L, L) for i in range(n)]
+    gens = [Symmetry(t1, k1), Symmetry(t2, k2), Symmetry(rot, rotation)]
+    if reflection is not None:
+        gens.append(Symmetry([triangular_index(i // L, i % L, L) for i in range(n)], reflection))
+    return gens
+
+
+def hypercube_bonds(dim: int) -> List[Tuple[int, int]]:
+    """Edges of the dim-dimensional hypercube (sites = dim-bit labels differing in one bit); for
+    dim = 4 this is the 4 x 4 square torus with its sites relabelled."""
+    return [(v, v ^ (1 << b)) for v in range(1 << dim) for b in range(dim) if v < v ^ (1 << b)]
+
+
+def hypercube_symmetries(dim: int, odd_permutations: int = 0, even_only: bool = False) -> List[Symmetry]:
+    """Automorphisms of the hypercube: the flip of label bit 0 and the permutations of the label
+    bits (2^dim * dim! elements), or only the even permutations of the label bits with
+    even_only=True.  odd_permutations=1 selects the representation that is -1 on odd permutations
+    of the label bits (else trivial)."""
+    n = 1 << dim
+
+    def relabel(p):  # site v -> the label whose bit p[b] is bit b of v
+        return [sum(((v >> b) & 1) << p[b] for b in range(dim)) for v in range(n)]
+
+    flip = Symmetry([v ^ 1 for v in range(n)], 0)
+    if even_only:
+        c1 = [1, 2, 0] + list(range(3, dim))
+        c2 = [0, 2, 3, 1] + list(range(4, dim))
+        return [flip, Symmetry(relabel(c1), 0), Symmetry(relabel(c2), 0)]
+    swap = [1, 0] + list(range(2, dim))
+    cycle = list(range(1, dim)) + [0]
+    # a dim-cycle is odd for even dim: sector dim/2 of its dim gives -1
+    return [flip, Symmetry(relabel(swap), odd_permutations),
+            Symmetry(relabel(cycle), (dim // 2) * odd_permutations if dim % 2 == 0 else 0)]
+
+
 def heisenberg(bonds: Sequence[Tuple[int, int]], J=1.0) -> Expr:
     """J * sum (σˣσˣ + σʸσʸ + σᶻσᶻ) over bonds (the form of chapel/data/heisenberg_*.yaml)."""
     e = Expr("σˣ₀ σˣ₁ + σʸ₀ σʸ₁ + σᶻ₀ σᶻ₁", sites=[list(b) for b in bonds])

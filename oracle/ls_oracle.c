@@ -67,6 +67,52 @@ static inline uint64_t image(const lso_group *g, int e, uint64_t x, int use_bene
   return use_benes ? apply_benes(g, e, x) : apply_perm(g, e, x);
 }
 
+/* Images of the W consecutive elements e0 .. e0 + W - 1 (W <= LSO_MAX_W): the reference's Halide
+ * kernels evaluate a chunk of W group elements as one vector (generator.cpp:80, :155-164); the
+ * lane loop below is written so that the compiler vectorises it the same way (the masks of one
+ * stage are contiguous over the elements, kernels.c:157-167). */
+#define LSO_MAX_W 16
+static inline void images_chunk_fixed(const lso_group *g, int e0, uint64_t x, uint64_t *out, const int W) {
+  uint64_t v[LSO_MAX_W];
+  for (int j = 0; j < W; ++j) v[j] = x;
+  for (int k = 0; k < g->depth; ++k) {
+    const uint64_t *m = g->masks + (int64_t)k * g->n_elems + e0;
+    const unsigned d = (unsigned)g->shifts[k];
+    for (int j = 0; j < W; ++j) {
+      const uint64_t y = ((v[j] >> d) ^ v[j]) & m[j];
+      v[j] = v[j] ^ y ^ (y << d);
+    }
+  }
+  for (int j = 0; j < W; ++j) out[j] = v[j];
+}
+
+static inline void images_chunk(const lso_group *g, int e0, int W, uint64_t x, int use_benes, uint64_t *out) {
+  if (!use_benes) {
+    for (int j = 0; j < W; ++j) out[j] = apply_perm(g, e0 + j, x);
+    return;
+  }
+  /* constant lane counts of the reference's builds: fully unrolled and vectorised */
+  if (W == 8) {
+    images_chunk_fixed(g, e0, x, out, 8);
+    return;
+  }
+  if (W == 4) {
+    images_chunk_fixed(g, e0, x, out, 4);
+    return;
+  }
+  uint64_t v[LSO_MAX_W];
+  for (int j = 0; j < LSO_MAX_W; ++j) v[j] = x;
+  for (int k = 0; k < g->depth; ++k) {
+    const uint64_t *m = g->masks + (int64_t)k * g->n_elems + e0;
+    const unsigned d = (unsigned)g->shifts[k];
+    for (int j = 0; j < W; ++j) {
+      const uint64_t y = ((v[j] >> d) ^ v[j]) & m[j];
+      v[j] = v[j] ^ y ^ (y << d);
+    }
+  }
+  for (int j = 0; j < W; ++j) out[j] = v[j];
+}
+
 /* ------------------------------------------------------------------------------------------ */
 /* state_info: generator.cpp:10-166.                                                            */
 /*   Per lane j < W: running (r, c, n) starting at (x, 1, 0); chunks m take element m*W + j.    */
@@ -99,24 +145,27 @@ static inline void si_elem(const lso_group *g, si_acc *a, uint64_t x, uint64_t y
 
 static si_acc state_info_one(const lso_group *g, int W, int use_benes, uint64_t x) {
   const int G = g->n_elems;
-  const int nchunks = G / W;
+  const int nchunks = W <= LSO_MAX_W ? G / W : 0;
+  si_acc lanes[LSO_MAX_W];
+  uint64_t img[LSO_MAX_W];
+  for (int j = 0; j < W && j < LSO_MAX_W; ++j) {
+    lanes[j].r = x; lanes[j].cre = 1.0; lanes[j].cim = 0.0; lanes[j].n = 0.0;
+  }
+  /* chunk m: lane j takes element m * W + j; each lane sees its elements in chunk order */
+  for (int m = 0; m < nchunks; ++m) {
+    images_chunk(g, m * W, W, x, use_benes, img);
+    for (int j = 0; j < W; ++j) si_elem(g, &lanes[j], x, img[j], m * W + j);
+  }
   si_acc total = {x, 1.0, 0.0, 0.0};
-  si_acc lane;
-  for (int j = 0; j < W; ++j) {
-    lane.r = x; lane.cre = 1.0; lane.cim = 0.0; lane.n = 0.0;
-    for (int m = 0; m < nchunks; ++m) {
-      int e = m * W + j;
-      si_elem(g, &lane, x, image(g, e, x, use_benes), e);
-    }
-    if (j == 0) {
-      total = lane;
-    } else {
-      if (lane.r < total.r) {
-        total.r = lane.r;
-        total.cre = lane.cre;
-        total.cim = lane.cim;
+  if (nchunks > 0) {
+    total = lanes[0];
+    for (int j = 1; j < W; ++j) {
+      if (lanes[j].r < total.r) {
+        total.r = lanes[j].r;
+        total.cre = lanes[j].cre;
+        total.cim = lanes[j].cim;
       }
-      total.n = total.n + lane.n;
+      total.n = total.n + lanes[j].n;
     }
   }
   for (int e = nchunks * W; e < G; ++e) si_elem(g, &total, x, image(g, e, x, use_benes), e);
@@ -173,40 +222,42 @@ static inline void ir_temp(const lso_group *g, uint64_t x, uint64_t y, int e, do
   }
 }
 
-void lso_is_representative(const lso_group *g, int lane_width, int use_benes, int64_t count,
-                           const uint64_t *xs, uint8_t *flags, double *norms) {
+static inline void is_rep_one(const lso_group *g, int W, int use_benes, uint64_t x, uint8_t *flag,
+                              double *norm) {
   const int G = g->n_elems;
-  const int W = lane_width;
-  const int nchunks = G / W;
-#pragma omp parallel for schedule(static)
-  for (int64_t i = 0; i < count; ++i) {
-    const uint64_t x = xs[i];
-    double sum = 0.0;
-    int ok = 1;
-    for (int m = 0; m < nchunks && ok; ++m) {
-      double ls = 0.0;
-      int lok = 1;
-      for (int j = 0; j < W; ++j) {
-        int e = m * W + j;
-        double s;
-        int ge;
-        ir_temp(g, x, image(g, e, x, use_benes), e, &s, &ge);
-        ls = ls + s;
-        lok = lok && ge;
-      }
-      sum = sum + ls;
-      ok = ok && lok;
-    }
-    for (int e = nchunks * W; e < G; ++e) {
+  const int nchunks = W <= LSO_MAX_W ? G / W : 0;
+  uint64_t img[LSO_MAX_W];
+  double sum = 0.0;
+  int ok = 1;
+  for (int m = 0; m < nchunks && ok; ++m) {
+    double ls = 0.0;
+    int lok = 1;
+    images_chunk(g, m * W, W, x, use_benes, img);
+    for (int j = 0; j < W; ++j) {
       double s;
       int ge;
-      ir_temp(g, x, image(g, e, x, use_benes), e, &s, &ge);
-      sum = sum + s;
-      ok = ok && ge;
+      ir_temp(g, x, img[j], m * W + j, &s, &ge);
+      ls = ls + s;
+      lok = lok && ge;
     }
-    norms[i] = sum;
-    flags[i] = (sum > 0) ? (uint8_t)ok : 0;
+    sum = sum + ls;
+    ok = ok && lok;
   }
+  for (int e = nchunks * W; e < G; ++e) {
+    double s;
+    int ge;
+    ir_temp(g, x, image(g, e, x, use_benes), e, &s, &ge);
+    sum = sum + s;
+    ok = ok && ge;
+  }
+  *norm = sum;
+  *flag = (sum > 0) ? (uint8_t)ok : 0;
+}
+
+void lso_is_representative(const lso_group *g, int lane_width, int use_benes, int64_t count,
+                           const uint64_t *xs, uint8_t *flags, double *norms) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < count; ++i) is_rep_one(g, lane_width, use_benes, xs[i], flags + i, norms + i);
 }
 
 /* Exact orbit data used by the checker where the reference's floating sums are exact:
@@ -342,6 +393,59 @@ int64_t lso_enumerate_projected(const lso_group *g, int lane_width, int use_bene
   return written_total;
 }
 
+/* Projected spin enumeration over [lower, upper] on all threads: the candidate range is split
+ * into pieces by combinadic rank (StatesEnumeration.chpl:130-189 splits it among tasks the same
+ * way), each piece walks its candidates in Gosper order (:29-32) and keeps a candidate iff
+ * is_representative flags it and its floating norm is positive (:242-268); the pieces are joined
+ * in order, so the output is sorted.  Returns the number of representatives (written up to cap). */
+int64_t lso_enumerate_projected_par(const lso_group *g, int lane_width, int use_benes, int hamming_fixed,
+                                    uint64_t lower, uint64_t upper, uint64_t *out, int64_t cap) {
+  if (lower > upper) return 0;
+  const int h = __builtin_popcountll(lower);
+  const int64_t r0 = hamming_fixed ? lso_fixed_hamming_state_to_index(lower) : (int64_t)lower;
+  const int64_t r1 = hamming_fixed ? lso_fixed_hamming_state_to_index(upper) : (int64_t)upper;
+  const int64_t n = r1 - r0 + 1;
+  int threads = 1;
+#ifdef _OPENMP
+  threads = omp_get_max_threads();
+#endif
+  int64_t pieces = (int64_t)threads * 64;
+  if (pieces > n) pieces = n;
+  uint64_t **bufs = (uint64_t **)calloc((size_t)pieces, sizeof(uint64_t *));
+  int64_t *lens = (int64_t *)calloc((size_t)pieces, sizeof(int64_t));
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t p = 0; p < pieces; ++p) {
+    const int64_t a = r0 + n * p / pieces, b = r0 + n * (p + 1) / pieces; /* ranks [a, b) */
+    int64_t cap_p = 1024, len = 0;
+    uint64_t *buf = (uint64_t *)malloc((size_t)cap_p * sizeof(uint64_t));
+    uint64_t v = hamming_fixed ? lso_fixed_hamming_index_to_state(a, h) : (uint64_t)a;
+    for (int64_t k = a; k < b; ++k) {
+      uint8_t flag;
+      double norm;
+      is_rep_one(g, lane_width, use_benes, v, &flag, &norm);
+      if (flag && norm > 0) {
+        if (len == cap_p) {
+          cap_p *= 2;
+          buf = (uint64_t *)realloc(buf, (size_t)cap_p * sizeof(uint64_t));
+        }
+        buf[len++] = v;
+      }
+      if (k + 1 < b) v = hamming_fixed ? next_fixed_hamming(v) : v + 1;
+    }
+    bufs[p] = buf;
+    lens[p] = len;
+  }
+  int64_t total = 0;
+  for (int64_t p = 0; p < pieces; ++p) {
+    for (int64_t k = 0; k < lens[p]; ++k, ++total)
+      if (total < cap) out[total] = bufs[p][k];
+    free(bufs[p]);
+  }
+  free(bufs);
+  free(lens);
+  return total;
+}
+
 /* Unprojected enumeration (StatesEnumeration.chpl:269-289): all states in [low, high] with
  * the Hamming weight of low (or all integers), with high clipped to high ^ mask under spin
  * inversion. */
@@ -447,6 +551,20 @@ static inline int64_t lso_index_one(const lso_index *c, uint64_t needle) {
   base += *base < needle;
   int64_t k = base - c->reps;
   return (k < c->number_states && *base == needle) ? k : -1;
+}
+
+/* Heap-allocated prefix index (built once per basis, as the reference keeps it in the basis'
+ * kernel data, reference.c:184-193). */
+lso_index *lso_index_create(const uint64_t *reps, int64_t n, int number_bits, int prefix_bits) {
+  lso_index *c = (lso_index *)malloc(sizeof(lso_index));
+  lso_index_init(c, reps, n, number_bits, prefix_bits);
+  return c;
+}
+
+void lso_index_destroy(lso_index *c) {
+  if (c == NULL) return;
+  lso_index_free(c);
+  free(c);
 }
 
 void lso_state_index(const lso_index *c, int64_t count, const uint64_t *xs, int64_t *out) {
@@ -613,6 +731,129 @@ int lso_matvec(const lso_group *g, const lso_projection *pr, int64_t D, const ui
     }
   }
   if (use_prefix) lso_index_free(&idx);
+  if (nnz_out) *nnz_out = nnz;
+  return error ? -1 : 0;
+}
+
+/* One column of the scatter (the per-column body of lso_matvec with x = e_j): calls emit(row,
+ * re, im) for the diagonal element and for every non-zero off-diagonal element; returns -1 if a
+ * non-zero element hit a state outside the basis, else the number of off-diagonal elements. */
+typedef struct {
+  int64_t *rows;
+  double *vals;
+  int64_t n;
+} lso_col_sink;
+
+static int64_t scatter_column(const lso_group *g, const lso_projection *pr, int64_t D, const uint64_t *reps,
+                              const lso_index *idx, const lso_terms *off, const lso_terms *diag, int mode,
+                              int64_t j, double na, double xre, double xim, lso_col_sink *sink, double *y) {
+  const int use_benes = (mode & LSO_BENES) != 0;
+  const int exact_norms = (mode & LSO_EXACT_NORMS) != 0;
+  const uint64_t a = reps[j];
+  int64_t found = 0;
+  if (pr->projection == 2 && na == 0.0) return 0; /* zero-norm representative: zero column */
+  if (diag != NULL && diag->n > 0) {
+    double accr = 0.0, acci = 0.0;
+    for (int t = 0; t < diag->n; ++t) {
+      if ((a & diag->m[t]) == diag->r[t]) {
+        int sign = 1 - 2 * (__builtin_popcountll(a & diag->s[t]) % 2);
+        accr += diag->v[2 * t] * (sign * xre) - diag->v[2 * t + 1] * (sign * xim);
+        acci += diag->v[2 * t] * (sign * xim) + diag->v[2 * t + 1] * (sign * xre);
+      }
+    }
+    if (sink) {
+      sink->rows[sink->n] = j;
+      sink->vals[2 * sink->n] = accr;
+      sink->vals[2 * sink->n + 1] = acci;
+      ++sink->n;
+    } else {
+#pragma omp atomic
+      y[2 * j] += accr;
+#pragma omp atomic
+      y[2 * j + 1] += acci;
+    }
+  }
+  if (off == NULL) return 0;
+  for (int t = 0; t < off->n; ++t) {
+    if ((a & off->m[t]) != off->r[t]) continue;
+    const int sign = 1 - 2 * (__builtin_popcountll(a & off->s[t]) % 2);
+    const double xr = sign * xre, xi = sign * xim;
+    const double cr = off->v[2 * t] * xr - off->v[2 * t + 1] * xi;
+    const double ci = off->v[2 * t] * xi + off->v[2 * t + 1] * xr;
+    const uint64_t beta = a ^ off->x[t];
+    uint64_t rep;
+    double chr, chi, nb;
+    project(g, pr, use_benes, exact_norms, beta, &rep, &chr, &chi, &nb);
+    const double sr = cr * nb / na, si = ci * nb / na;
+    const double outr = chr * sr - chi * si, outi = chr * si + chi * sr;
+    if (outr == 0.0 && outi == 0.0) continue;
+    int64_t i;
+    if (pr->state_index_identity)
+      i = (int64_t)rep;
+    else
+      i = idx != NULL ? lso_index_one(idx, rep) : bsearch_index(reps, D, rep);
+    if (i < 0) return -1;
+    ++found;
+    if (sink) {
+      sink->rows[sink->n] = i;
+      sink->vals[2 * sink->n] = outr;
+      sink->vals[2 * sink->n + 1] = outi;
+      ++sink->n;
+    } else {
+#pragma omp atomic
+      y[2 * i] += outr;
+#pragma omp atomic
+      y[2 * i + 1] += outi;
+    }
+  }
+  return found;
+}
+
+/* Columns cols[0..ncols) of H (complex arithmetic), element by element: column c writes its
+ * elements (the diagonal one first) to rows[c * stride + k] and the complex values to
+ * vals[2 * (c * stride + k) + {0, 1}], k < counts[c], stride = off->n + 1; col_norms[c] is the
+ * norm of representative cols[c].  Returns 0, or -1 if an element hit a state outside the basis. */
+int lso_matvec_columns(const lso_group *g, const lso_projection *pr, int64_t D, const uint64_t *reps,
+                       const lso_index *idx, const lso_terms *off, const lso_terms *diag, int mode, int64_t ncols,
+                       const int64_t *cols, const double *col_norms, int64_t *rows, double *vals,
+                       int64_t *counts) {
+  const int64_t stride = (off != NULL ? off->n : 0) + 1;
+  int error = 0;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t c = 0; c < ncols; ++c) {
+    lso_col_sink sink = {rows + c * stride, vals + 2 * c * stride, 0};
+    const double na = pr->projection == 2 ? col_norms[c] : 1.0;
+    if (scatter_column(g, pr, D, reps, idx, off, diag, mode, cols[c], na, 1.0, 0.0, &sink, NULL) < 0) {
+#pragma omp atomic write
+      error = 1;
+    }
+    counts[c] = sink.n;
+  }
+  return error ? -1 : 0;
+}
+
+/* The reference's scatter over a sample of columns (DistributedMatrixVector.chpl:91-143 with
+ * BatchedOperator.chpl:139-253): y[i] += H[i, cols[c]] * x[c] with relaxed atomic adds, all
+ * threads, complex x and y (y has D entries and is not cleared).  *nnz_out = off-diagonal
+ * elements generated.  Returns 0, or -1 if an element hit a state outside the basis. */
+int lso_matvec_sample(const lso_group *g, const lso_projection *pr, int64_t D, const uint64_t *reps,
+                      const lso_index *idx, const lso_terms *off, const lso_terms *diag, int mode, int64_t ncols,
+                      const int64_t *cols, const double *col_norms, const double *x, double *y,
+                      int64_t *nnz_out) {
+  int64_t nnz = 0;
+  int error = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : nnz)
+  for (int64_t c = 0; c < ncols; ++c) {
+    const double na = pr->projection == 2 ? col_norms[c] : 1.0;
+    const int64_t f = scatter_column(g, pr, D, reps, idx, off, diag, mode, cols[c], na, x[2 * c], x[2 * c + 1],
+                                     NULL, y);
+    if (f < 0) {
+#pragma omp atomic write
+      error = 1;
+    } else {
+      nnz += f;
+    }
+  }
   if (nnz_out) *nnz_out = nnz;
   return error ? -1 : 0;
 }

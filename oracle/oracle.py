@@ -85,6 +85,22 @@ def lib():
         L.lso_matvec.argtypes = [POINTER(lso_group), POINTER(lso_projection), c_int64, POINTER(c_uint64),
                                  POINTER(c_double), POINTER(lso_terms), POINTER(lso_terms), c_int,
                                  POINTER(c_double), POINTER(c_double), c_int64, c_int64, POINTER(c_int64)]
+        L.lso_enumerate_projected_par.restype = c_int64
+        L.lso_enumerate_projected_par.argtypes = [POINTER(lso_group), c_int, c_int, c_int, c_uint64, c_uint64,
+                                                  POINTER(c_uint64), c_int64]
+        L.lso_index_create.restype = c_void_p
+        L.lso_index_create.argtypes = [POINTER(c_uint64), c_int64, c_int, c_int]
+        L.lso_index_destroy.argtypes = [c_void_p]
+        L.lso_matvec_columns.restype = c_int
+        L.lso_matvec_columns.argtypes = [POINTER(lso_group), POINTER(lso_projection), c_int64, POINTER(c_uint64),
+                                         c_void_p, POINTER(lso_terms), POINTER(lso_terms), c_int, c_int64,
+                                         POINTER(c_int64), POINTER(c_double), POINTER(c_int64), POINTER(c_double),
+                                         POINTER(c_int64)]
+        L.lso_matvec_sample.restype = c_int
+        L.lso_matvec_sample.argtypes = [POINTER(lso_group), POINTER(lso_projection), c_int64, POINTER(c_uint64),
+                                        c_void_p, POINTER(lso_terms), POINTER(lso_terms), c_int, c_int64,
+                                        POINTER(c_int64), POINTER(c_double), POINTER(c_double), POINTER(c_double),
+                                        POINTER(c_int64)]
         L.lso_max_threads.restype = c_int
         L.lso_set_threads.argtypes = [c_int]
         _lib = L
@@ -178,6 +194,95 @@ def enumerate_projected(g: Group, lower, upper, hamming_fixed=True, lane_width=4
     if n > cap:
         return enumerate_projected(g, lower, upper, hamming_fixed, lane_width, use_benes, cap=int(n))
     return out[:n]
+
+
+def enumerate_projected_par(g: Group, lower, upper, hamming_fixed=True, lane_width=8, use_benes=True, cap=None):
+    """Projected enumeration on all threads (ls_oracle.c lso_enumerate_projected_par): the same
+    states as enumerate_projected, with the candidate range split among threads by rank."""
+    if cap is None:
+        n_cand = rank(upper) - rank(lower) + 1 if hamming_fixed else upper - lower + 1
+        cap = max(16, int(n_cand // max(1, g.order) * 3 // (2 if g.spin_inversion else 1)) + 4096)
+        cap = min(cap, int(n_cand) + 1)
+    out = np.zeros(cap, dtype=np.uint64)
+    n = lib().lso_enumerate_projected_par(ctypes.byref(g.c), lane_width, int(use_benes), int(hamming_fixed),
+                                          lower, upper, _p(out, c_uint64), cap)
+    if n > cap:
+        return enumerate_projected_par(g, lower, upper, hamming_fixed, lane_width, use_benes, cap=int(n))
+    return out[:n]
+
+
+class Index:
+    """The reference's prefix-table index over sorted representatives (kernels/indexing.c:45-117),
+    built once; keeps a reference to the array it indexes."""
+
+    def __init__(self, reps, number_bits, prefix_bits=22):
+        self.reps = np.ascontiguousarray(reps, dtype=np.uint64)
+        self.ptr = lib().lso_index_create(_p(self.reps, c_uint64), self.reps.shape[0], int(number_bits),
+                                          int(prefix_bits))
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            lib().lso_index_destroy(self.ptr)
+            self.ptr = None
+
+
+def _projection(projection, spin_inversion, n_bits, identity_index=False):
+    pr = lso_projection()
+    pr.projection = projection
+    pr.spin_inversion = spin_inversion
+    pr.n_bits = n_bits
+    pr.state_index_identity = int(identity_index)
+    return pr
+
+
+def matvec_columns(g, projection, spin_inversion, n_bits, reps, cols, col_norms, off: "Terms", diag: "Terms",
+                   baseline=False, exact_norms=True, index: "Index" = None, identity_index=False):
+    """Columns `cols` of H as sparse lists (ls_oracle.c lso_matvec_columns): returns a list of
+    (rows, values) per column, complex values, the diagonal element first, duplicates not merged.
+    baseline: Benes orbit scan (else the bit-by-bit permutations)."""
+    reps = np.ascontiguousarray(reps, dtype=np.uint64)
+    cols = np.ascontiguousarray(cols, dtype=np.int64)
+    nc = cols.shape[0]
+    norms = np.ascontiguousarray(np.ones(nc) if col_norms is None else col_norms, dtype=np.float64)
+    stride = off.c.n + 1
+    rows = np.zeros(nc * stride, dtype=np.int64)
+    vals = np.zeros(2 * nc * stride, dtype=np.float64)
+    counts = np.zeros(nc, dtype=np.int64)
+    if g is None:
+        g = Group(np.zeros((0, 1)), [], [], 0, n_bits)
+    pr = _projection(projection, spin_inversion, n_bits, identity_index)
+    mode = (LSO_BENES if baseline else 0) | (LSO_EXACT_NORMS if exact_norms else 0)
+    st = lib().lso_matvec_columns(ctypes.byref(g.c), ctypes.byref(pr), reps.shape[0], _p(reps, c_uint64),
+                                  index.ptr if index is not None else None, ctypes.byref(off.c),
+                                  ctypes.byref(diag.c), mode, nc, _p(cols, c_int64), _p(norms, c_double),
+                                  _p(rows, c_int64), _p(vals, c_double), _p(counts, c_int64))
+    if st != 0:
+        raise RuntimeError("an element of a sampled column left the basis")
+    v = vals.view(np.complex128)
+    return [(rows[c * stride:c * stride + counts[c]].copy(), v[c * stride:c * stride + counts[c]].copy())
+            for c in range(nc)]
+
+
+def matvec_sample(g, projection, spin_inversion, n_bits, reps, cols, col_norms, off: "Terms", diag: "Terms", x, y,
+                  index: "Index", exact_norms=False):
+    """y += H[:, cols] x over a sample of columns by the reference's scatter algorithm with atomics
+    (ls_oracle.c lso_matvec_sample), Benes orbit scan and prefix index; x complex [len(cols)],
+    y complex [D] (not cleared).  Returns the number of off-diagonal elements generated."""
+    reps = index.reps if index is not None else np.ascontiguousarray(reps, dtype=np.uint64)
+    cols = np.ascontiguousarray(cols, dtype=np.int64)
+    norms = np.ascontiguousarray(col_norms, dtype=np.float64)
+    xv = np.ascontiguousarray(x, dtype=np.complex128).view(np.float64)
+    assert y.dtype == np.complex128 and y.flags.c_contiguous and y.shape[0] == reps.shape[0]
+    pr = _projection(projection, spin_inversion, n_bits)
+    mode = LSO_BENES | LSO_PREFIX_INDEX | LSO_ATOMIC | (LSO_EXACT_NORMS if exact_norms else 0)
+    nnz = c_int64(0)
+    st = lib().lso_matvec_sample(ctypes.byref(g.c), ctypes.byref(pr), reps.shape[0], _p(reps, c_uint64),
+                                 index.ptr if index is not None else None, ctypes.byref(off.c), ctypes.byref(diag.c),
+                                 mode, cols.shape[0], _p(cols, c_int64), _p(norms, c_double), _p(xv, c_double),
+                                 _p(y.view(np.float64), c_double), ctypes.byref(nnz))
+    if st != 0:
+        raise RuntimeError("an element of a sampled column left the basis")
+    return int(nnz.value)
 
 
 def enumerate_unprojected(number_sites, spin_inversion, hamming_fixed, low, high):
