@@ -1283,10 +1283,11 @@ extern "C" int ls_gpu_autotune_matvec(ls_hs_operator const* op, int k, int* best
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  const int threads_choices[] = {256, 320};
-  const int wave_choices[] = {1, 2, 4, 8};
+  // threads per CTA (each kernel clamps to its own maximum; 0 = that maximum) x grid waves
+  const int threads_choices[] = {0, 320, 512};
+  const int wave_choices[] = {1, 2, 4};
   double best = 1e300;
-  int bt = 256, bw = 2, rc = 0;
+  int bt = 0, bw = 1, rc = 0;
   for (int th : threads_choices) {
     for (int wv : wave_choices) {
       set_matvec_config(th, wv);

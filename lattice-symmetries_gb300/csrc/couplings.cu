@@ -23,7 +23,6 @@ __global__ void __launch_bounds__(256, 2)
                         const uint64_t* __restrict__ binom) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr unsigned FULL = 0xffffffffu;
-  constexpr int Gp = 32 * GPL;
   const PackedTables T = stage_packed(p, L, smem, true);
   int32_t* cpl_off = (int32_t*)(smem + off_cpl);
   int32_t* cpl_diag = cpl_off + p.off.n;
@@ -34,8 +33,8 @@ __global__ void __launch_bounds__(256, 2)
   const int nbits = p.group.n_bits;
   const int SH = 64 - nbits;
   const uint64_t lowmask = (1ull << SH) - 1;
-  const uint64_t flipkey = ((~0ull >> SH) << SH) | 1ull;
-  const uint64_t* ohl = T.oh + lane;
+  const ScanKeys keys = scan_keys(nbits);
+  uint32_t* gw = T.ga + (threadIdx.x >> 5) * 32 * rec_stride(GPL);  // this warp's g.a records
   const double2* X = reinterpret_cast<const double2*>(x);
   const double2* Gv = reinterpret_cast<const double2*>(g);
   const DeviceIndex& ix = p.index;
@@ -72,16 +71,9 @@ __global__ void __launch_bounds__(256, 2)
       }
     }
 
-    uint64_t ga[GPL];
-#pragma unroll
-    for (int k = 0; k < GPL; ++k) ga[k] = 0;
-    for (uint64_t bits = a; bits != 0; bits &= bits - 1) {
-      const uint64_t* r = ohl + (__ffsll((long long)bits) - 1) * Gp;
-#pragma unroll
-      for (int k = 0; k < GPL; ++k) ga[k] ^= r[32 * k];
-    }
-#pragma unroll
-    for (int k = 0; k < GPL; ++k) ga[k] |= (uint64_t)(2 * (lane + 32 * k));
+    __syncwarp();  // the previous row's scans have read the records
+    uint32_t gh[GPL];
+    row_images<GPL>(T.rec, gw, a, lane, gh);
 
     // the owning lane of each element keeps its key and term; coefficient, sign and coupling
     // are read at the flush
@@ -124,34 +116,12 @@ __global__ void __launch_bounds__(256, 2)
             continue;
           }
         }
-        uint64_t cand[GPL];
-        if (((info >> 16) & 0xffu) == 2u) {  // two flipped sites: their images directly
-          const uint64_t* r0 = ohl + (int)(info & 0xffu) * Gp;
-          const uint64_t* r1 = ohl + (int)((info >> 8) & 0xffu) * Gp;
-#pragma unroll
-          for (int k = 0; k < GPL; ++k) {
-            cand[k] = ga[k] ^ r0[32 * k] ^ r1[32 * k];
-            if (INV) cand[k] = flip_packed(cand[k], flipkey);
-          }
-        } else {
-#pragma unroll
-          for (int k = 0; k < GPL; ++k) {
-            uint64_t v = ga[k];
-            for (uint64_t bits = xt; bits != 0; bits &= bits - 1)
-              v ^= ohl[(__ffsll((long long)bits) - 1) * Gp + 32 * k];
-            cand[k] = INV ? flip_packed(v, flipkey) : v;
-          }
-        }
-#pragma unroll
-        for (int w2 = 1; w2 < GPL; w2 *= 2) {
-#pragma unroll
-          for (int k = 0; k + w2 < GPL; k += 2 * w2) cand[k] = cand[k + w2] < cand[k] ? cand[k + w2] : cand[k];
-        }
-        const uint32_t hi = (uint32_t)(cand[0] >> 32), lo = (uint32_t)cand[0];
-        const uint32_t mhi = __reduce_min_sync(FULL, hi);
-        const uint32_t mlo = __reduce_min_sync(FULL, hi == mhi ? lo : 0xffffffffu);
+        const uint64_t key = (((info >> 16) & 0xffu) == 2u)
+                                 ? scan_two_site<GPL, INV>(T.rec, gw, gh, (int)(info & 0xffu),
+                                                           (int)((info >> 8) & 0xffu), lane, keys)
+                                 : scan_general<GPL, INV>(T.rec, gw, gh, xt, lane, keys);
         if (lane == nslot) {
-          my_key = ((uint64_t)mhi << 32) | mlo;
+          my_key = key;
           my_t = t;
         }
         if (++nslot == 32) {
@@ -209,10 +179,10 @@ int launch_coupling_products(const MatvecProblem& p, int nc, const double* d_g, 
   if (p.off.coupling == nullptr) return fail(LS_GPU_ERR_INVALID, "operator terms carry no coupling ids");
   const uint64_t* binom = device_binomials();
   if (binom == nullptr) return LS_GPU_ERR_CUDA;
-  const PackedLayout L = make_packed_layout(p);
+  const PackedLayout L = make_packed_layout(p, 0, 256);
   const size_t off_cpl = (L.total + 15) & ~(size_t)15;
   const size_t smem = off_cpl + (size_t)(p.off.n + p.diag.n) * 4;
-  if (smem > 200 * 1024) return fail(LS_GPU_ERR_INVALID, "term tables too large for shared memory");
+  if (smem > kMaxDynamicSmem) return fail(LS_GPU_ERR_INVALID, "term tables too large for shared memory");
   const int blocks = std::max(1, std::min(num_sms() * 8, (int)((p.n_rows + 7) / 8)));
   double2* partial = (double2*)scratch((size_t)blocks * nc * sizeof(double2), 6);
   if (partial == nullptr) return LS_GPU_ERR_CUDA;

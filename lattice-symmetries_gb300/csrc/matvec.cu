@@ -1,33 +1,31 @@
 // matvec.cu -- launch policy of the gather kernels (kernel choice, grid shape, RHS blocking).
 #include <algorithm>
 
-#include "matvec_dispatch.h"
-#include "matvec_impl.cuh"
+#include "matvec_launch.cuh"
 
 namespace lsg {
 
-int launch_packed(bool cplx, int k, int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L,
-                  LaunchShape sh, const double* x, int64_t ldx, double* y, int64_t ldy, int* err,
-                  const uint64_t* binom, cudaStream_t s) {
+int launch_packed(bool cplx, int k, int gpl, bool inv, const MatvecProblem& p, const double* x, int64_t ldx,
+                  double* y, int64_t ldy, int* err, const uint64_t* binom, cudaStream_t s) {
   if (p.group.fermionic) {
     if (inv) return fail(LS_GPU_ERR_INVALID, "fermionic groups have no spin inversion");
-    return launch_packed_fermi(cplx, k, gpl, p, L, sh, x, ldx, y, ldy, err, binom, s);
+    return launch_packed_fermi(cplx, k, gpl, p, x, ldx, y, ldy, err, binom, s);
   }
   if (!cplx) {
     switch (k) {
-      case 1: return launch_packed_real(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
-      case 2: return launch_packed_real_k2(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
-      case 4: return launch_packed_real_k4(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
-      case 8: return launch_packed_real_k8(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
-      case 16: return launch_packed_real_k16(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
+      case 1: return launch_packed_real(gpl, inv, p, x, ldx, y, ldy, err, binom, s);
+      case 2: return launch_packed_real_k2(gpl, inv, p, x, ldx, y, ldy, err, binom, s);
+      case 4: return launch_packed_real_k4(gpl, inv, p, x, ldx, y, ldy, err, binom, s);
+      case 8: return launch_packed_real_k8(gpl, inv, p, x, ldx, y, ldy, err, binom, s);
+      case 16: return launch_packed_real_k16(gpl, inv, p, x, ldx, y, ldy, err, binom, s);
       default: return LS_GPU_ERR_INVALID;
     }
   }
   switch (k) {
-    case 1: return launch_packed_cplx_k1(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
-    case 4: return launch_packed_cplx_k4(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
-    case 8: return launch_packed_cplx_k8(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
-    case 16: return launch_packed_cplx_k16(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
+    case 1: return launch_packed_cplx_k1(gpl, inv, p, x, ldx, y, ldy, err, binom, s);
+    case 4: return launch_packed_cplx_k4(gpl, inv, p, x, ldx, y, ldy, err, binom, s);
+    case 8: return launch_packed_cplx_k8(gpl, inv, p, x, ldx, y, ldy, err, binom, s);
+    case 16: return launch_packed_cplx_k16(gpl, inv, p, x, ldx, y, ldy, err, binom, s);
     default: return LS_GPU_ERR_INVALID;
   }
 }
@@ -37,8 +35,9 @@ static int g_blocks_per_sm_override = 0;
 static int g_rhs_tile = 16;  // most right-hand sides per launch (16, 8, 4 or 1)
 
 int set_matvec_config(int threads, int blocks_per_sm) {
-  // the warp-per-row kernels are compiled for at most 320 threads per block
-  if (threads != 0 && (threads < 32 || threads > 320 || threads % 32 != 0)) return LS_GPU_ERR_INVALID;
+  // the warp-per-row kernels are compiled for at most 768 threads per block (each kernel clamps
+  // the setting to its own maximum)
+  if (threads != 0 && (threads < 32 || threads > 768 || threads % 32 != 0)) return LS_GPU_ERR_INVALID;
   if (blocks_per_sm < 0 || blocks_per_sm > 64) return LS_GPU_ERR_INVALID;
   g_threads_override = threads;
   g_blocks_per_sm_override = blocks_per_sm;
@@ -67,9 +66,10 @@ int get_block_arithmetic() { return g_block_pairs; }
 
 static bool use_pairs(int gpl) { return g_block_pairs == 2 || (g_block_pairs == 1 && gpl <= 2); }
 
+// threads 0: each kernel's own maximum; waves: grid = SMs x resident CTAs per SM x waves.
 void get_matvec_config(int* threads, int* waves, int* rhs_tile) {
-  if (threads) *threads = g_threads_override > 0 ? g_threads_override : 320;
-  if (waves) *waves = g_blocks_per_sm_override > 0 ? g_blocks_per_sm_override : 8;
+  if (threads) *threads = g_threads_override;
+  if (waves) *waves = g_blocks_per_sm_override > 0 ? g_blocks_per_sm_override : 1;
   if (rhs_tile) *rhs_tile = g_rhs_tile;
 }
 
@@ -100,17 +100,32 @@ __global__ void k_prescale_pairs(const double2* __restrict__ x, int64_t ldx, con
   }
 }
 
-constexpr size_t kMaxDynamicSmem = 200 * 1024;
+int packed_launch_shape(const void* kern, int max_threads, const MatvecProblem& p, int n_sectors, int64_t rows,
+                        LaunchShape* sh, PackedLayout* L) {
+  const int waves = g_blocks_per_sm_override > 0 ? g_blocks_per_sm_override : 1;
+  int threads = g_threads_override > 0 ? std::min(g_threads_override, max_threads) : max_threads;
+  for (; threads >= 64; threads -= 32) {
+    *L = make_packed_layout(p, n_sectors, threads);
+    if (L->total > kMaxDynamicSmem) continue;
+    if (!ensure_smem_limit(kern, L->total)) return LS_GPU_ERR_CUDA;
+    int resident = 0;
+    if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, threads, L->total),
+                 "occupancy of a packed kernel"))
+      return LS_GPU_ERR_CUDA;
+    if (resident < 1) continue;
+    const int warps = threads / 32;
+    int64_t blocks = (int64_t)num_sms() * resident * waves;
+    blocks = std::min<int64_t>(blocks, (rows + warps - 1) / warps);
+    *sh = LaunchShape{(int)std::max<int64_t>(blocks, 1), threads};
+    return 0;
+  }
+  return fail(LS_GPU_ERR_INVALID, "packed matvec tables do not fit in shared memory");
+}
 
-LaunchShape packed_shape(int64_t n_rows) {
-  // two resident CTAs per SM; `waves` grids of that size balance the uneven per-row work
-  const int threads = g_threads_override > 0 ? g_threads_override : 320;
-  const int waves = g_blocks_per_sm_override > 0 ? g_blocks_per_sm_override : 8;
-  const int warps_per_block = threads / 32;
-  int64_t blocks = (int64_t)num_sms() * 2 * waves;
-  blocks = std::min<int64_t>(blocks, (n_rows + warps_per_block - 1) / warps_per_block);
-  blocks = std::max<int64_t>(blocks, 1);
-  return LaunchShape{(int)blocks, threads};
+// The packed tables fit in shared memory with at least two warps per CTA.
+static bool packed_fits(const MatvecProblem& p, int n_sectors = 0) {
+  return p.group.gpl > 0 && p.group.onehot_packed != nullptr &&
+         make_packed_layout(p, n_sectors, 64).total <= kMaxDynamicSmem;
 }
 
 // Which kernel launch_matvec runs for `p`: 2 packed projected (*gpl = slots per lane), 1 the
@@ -118,8 +133,7 @@ LaunchShape packed_shape(int64_t n_rows) {
 int matvec_kernel_form(const MatvecProblem& p, int* gpl) {
   *gpl = 0;
   if (p.projection != 2) return 0;
-  const PackedLayout PL = make_packed_layout(p);
-  if (p.group.gpl > 0 && p.group.onehot_packed != nullptr && PL.total <= kMaxDynamicSmem) {
+  if (packed_fits(p)) {
     *gpl = p.group.gpl;
     return 2;
   }
@@ -137,10 +151,7 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
   const size_t scalar_words = cplx ? 2 : 1;  // doubles per element
   if (p.projection == 2) {
     const bool inv = p.group.spin_inversion != 0;
-    const LaunchShape sh = packed_shape(p.n_rows);
-    const PackedLayout PL = make_packed_layout(p);
-    const bool packed = p.group.gpl > 0 && p.group.onehot_packed != nullptr && PL.total <= kMaxDynamicSmem;
-    if (packed) {
+    if (packed_fits(p)) {
       // Right-hand-side chunks of 16, 8, 4 and 1 columns; complex chunks of 8 or 16 run the
       // FP32-pair kernels (g_block_pairs).
       std::vector<int> chunks;
@@ -201,10 +212,10 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
         double* ys = d_y + (size_t)done * scalar_words;
         if (d_xp != nullptr && chunk >= 8) {
           q.xs = reinterpret_cast<const double*>(d_xp + done);
-          rc = launch_packed_pair(chunk, p.group.gpl, inv, q, PL, sh, xs, ldx, ys, ldy, d_err, binom, s);
+          rc = launch_packed_pair(chunk, p.group.gpl, inv, q, xs, ldx, ys, ldy, d_err, binom, s);
         } else {
           q.xs = d_xs ? d_xs + (size_t)done * scalar_words : nullptr;
-          rc = launch_packed(cplx, chunk, p.group.gpl, inv, q, PL, sh, xs, ldx, ys, ldy, d_err, binom, s);
+          rc = launch_packed(cplx, chunk, p.group.gpl, inv, q, xs, ldx, ys, ldy, d_err, binom, s);
         }
         if (rc != 0) break;
         done += chunk;
@@ -219,8 +230,9 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
     if (gpl < 0) return fail(LS_GPU_ERR_INVALID, "symmetry group too large for the matvec kernels");
     const SmemLayout L = make_layout(p, true);
     if (L.total > kMaxDynamicSmem) return fail(LS_GPU_ERR_INVALID, "term tables too large for shared memory");
-    // the fallback kernel is compiled for at most 256 threads per block
-    const LaunchShape shf{(int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sh.blocks * sh.threads / 256,
+    // the fallback kernel is compiled for at most 256 threads per block (two CTAs per SM)
+    const int waves = g_blocks_per_sm_override > 0 ? g_blocks_per_sm_override : 8;
+    const LaunchShape shf{(int)std::max<int64_t>(1, std::min<int64_t>((int64_t)num_sms() * 2 * waves,
                                                                       (p.n_rows + 7) / 8)),
                           256};
     for (int c = 0; c < k; ++c) {
@@ -251,7 +263,6 @@ struct SectorPlan {
   bool batched = false;      // the sectors can share one launch
   bool use_batched = true;   // ... and run() does so (else one launch per sector)
   MatvecProblem shared{};          // tables of the first sector (batched form)
-  PackedLayout layout{};
   int64_t total_rows = 0;
   struct Chunk {
     int k;
@@ -282,8 +293,7 @@ int sector_plan_build(const std::vector<MatvecProblem>& problems, bool shareable
                   p0.group.gpl <= kSectorMaxGpl && p0.group.onehot_packed != nullptr;
   if (plan->batched) {
     plan->shared = p0;
-    plan->layout = make_packed_layout(p0, n);
-    if (plan->layout.total > kMaxDynamicSmem) plan->batched = false;
+    if (!packed_fits(p0, n)) plan->batched = false;
   }
   if (plan->batched) {
     std::vector<SectorDesc> h(n);
@@ -360,7 +370,6 @@ int sector_plan_run(const SectorPlan* plan, int* d_err, cudaStream_t s) {
   const uint64_t* binom = device_binomials();
   if (binom == nullptr) return LS_GPU_ERR_CUDA;
   if (plan->total_rows == 0) return 0;
-  const LaunchShape sh = packed_shape(plan->total_rows);
   const bool inv = plan->shared.group.spin_inversion != 0;
   // chunks of 8 or 16 columns run the FP32-pair kernels from a prescaled pair copy of all
   // sectors' columns (one streaming pass); the others gather x and the norms in FP64
@@ -388,11 +397,11 @@ int sector_plan_run(const SectorPlan* plan, int* d_err, cudaStream_t s) {
   int rc = 0;
   for (const SectorPlan::Chunk& c : plan->chunks) {
     if (d_xp != nullptr && c.k >= 8)
-      rc = launch_sectors_pair(c.k, plan->shared.group.gpl, inv, plan->shared, plan->layout, sh, c.d_desc,
+      rc = launch_sectors_pair(c.k, plan->shared.group.gpl, inv, plan->shared, plan->n_sectors, c.d_desc,
                                plan->n_sectors, plan->total_rows, plan->ldx, plan->ldy, d_err, binom,
                                reinterpret_cast<const double*>(d_xp), plan->k, c.col, s);
     else
-      rc = launch_sectors(c.k, plan->shared.group.gpl, inv, plan->shared, plan->layout, sh, c.d_desc,
+      rc = launch_sectors(c.k, plan->shared.group.gpl, inv, plan->shared, plan->n_sectors, c.d_desc,
                           plan->n_sectors, plan->total_rows, plan->ldx, plan->ldy, d_err, binom, nullptr, 0, 0, s);
     if (rc != 0) break;
   }

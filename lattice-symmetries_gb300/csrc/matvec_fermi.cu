@@ -7,25 +7,22 @@
 
 namespace lsg {
 
-int launch_packed_fermi(bool cplx, int k, int gpl, const MatvecProblem& p, const PackedLayout& L, LaunchShape sh,
-                        const double* x, int64_t ldx, double* y, int64_t ldy, int* err, const uint64_t* binom,
-                        cudaStream_t s) {
+int launch_packed_fermi(bool cplx, int k, int gpl, const MatvecProblem& p, const double* x, int64_t ldx, double* y,
+                        int64_t ldy, int* err, const uint64_t* binom, cudaStream_t s) {
   auto with_k = [&](auto gtag) -> int {
     constexpr int G = decltype(gtag)::value;
+    auto go = [&](auto kern, int max_threads) {
+      return launch_packed_kernel(kern, max_threads, "k_matvec_packed<fermi>", p, x, ldx, y, ldy, err, binom, s);
+    };
     if (!cplx) {
       if (k != 1) return LS_GPU_ERR_INVALID;
-      return launch_with_smem(k_matvec_packed<G, false, false, 1, true>, "k_matvec_packed<fermi>", p, L, sh, x,
-                              ldx, y, ldy, err, binom, s);
+      return go(k_matvec_packed<G, false, false, 1, true>, PackedBounds<G, 1, false>::threads);
     }
     switch (k) {
-      case 1: return launch_with_smem(k_matvec_packed<G, false, true, 1, true>, "k_matvec_packed<fermi>", p, L, sh,
-                                      x, ldx, y, ldy, err, binom, s);
-      case 4: return launch_with_smem(k_matvec_packed<G, false, true, 4, true>, "k_matvec_packed<fermi>", p, L, sh,
-                                      x, ldx, y, ldy, err, binom, s);
-      case 8: return launch_with_smem(k_matvec_packed<G, false, true, 8, true>, "k_matvec_packed<fermi>", p, L, sh,
-                                      x, ldx, y, ldy, err, binom, s);
-      case 16: return launch_with_smem(k_matvec_packed<G, false, true, 16, true>, "k_matvec_packed<fermi>", p, L,
-                                       sh, x, ldx, y, ldy, err, binom, s);
+      case 1: return go(k_matvec_packed<G, false, true, 1, true>, PackedBounds<G, 1, false>::threads);
+      case 4: return go(k_matvec_packed<G, false, true, 4, true>, PackedBounds<G, 4, false>::threads);
+      case 8: return go(k_matvec_packed<G, false, true, 8, true>, PackedBounds<G, 8, false>::threads);
+      case 16: return go(k_matvec_packed<G, false, true, 16, true>, PackedBounds<G, 16, false>::threads);
       default: return LS_GPU_ERR_INVALID;
     }
   };

@@ -384,19 +384,28 @@ __global__ void __launch_bounds__(256, 2)
 // ------------------------------------------------------------------------------------------------
 // Packed projected kernel (default for projected bases).
 //
-// Same gather as k_matvec_projected, with three changes that cut the integer work per generated
-// element about fourfold:
+// Same gather as k_matvec_projected, with a cheaper orbit scan:
 //  * the site-image table is pre-shifted to the top bits and padded to GPL*32 slots, and the low
-//    bits of every lane's g.a carry the candidate index 2*slot, so one unsigned 64-bit minimum
+//    bits of every lane's g.a carry the candidate index 2*slot, so the minimum of the 64-bit keys
 //    gives the representative and its group element together, and the spin flip is a sign-mask
 //    XOR that also sets the flip bit of the index;
-//  * a slot's table entries sit at immediate offsets 32*k from the lane's base, and two-site terms
-//    read their two rows directly;
+//  * the minimum is found in two passes (scan_two_site): the high 32 bits of every candidate
+//    first (one three-input XOR and a min -- with spin inversion also a max -- per slot), then the
+//    exact 64-bit keys of the few candidates whose high word ties the warp minimum;
 //  * the terms matching the row are found with one ballot per 32 terms.
 // The row sum is divided by n_i once at the end.
+//
+// Site images in shared memory are kept as lane records: slot j of lane L (group element
+// e = L + 32 j) of site r is stored as its (lo, hi) 32-bit words at
+// rec[(r * 32 + L) * S + 2 j + {0, 1}], S = 2 GPL + 1.  S is odd, so the 32 lanes reading one slot
+// of their own records hit 32 distinct banks, and lanes j < GPL reading the slots of one lane's
+// record read consecutive words.  Each warp also keeps the images of its current row state
+// (g.a, with the candidate index in the low bits) in a record area of the same layout.
 // ------------------------------------------------------------------------------------------------
+__host__ __device__ constexpr int rec_stride(int gpl) { return 2 * gpl + 1; }
+
 struct PackedLayout {
-  size_t off_onehot, off_chars, off_tm, off_tl, off_tx, off_ts, off_tv, off_ti, off_dm, off_dr, off_ds, off_dv;
+  size_t off_rec, off_ga, off_chars, off_tm, off_tl, off_tx, off_ts, off_tv, off_ti, off_dm, off_dr, off_ds, off_dv;
   size_t off_sectors;  // sector table of the batched kernel (n_sectors > 0)
   size_t off_fsign;    // fermionic sign tables [n_bits][gpl * 32] (fermionic groups)
   size_t total;
@@ -416,12 +425,16 @@ struct SectorDesc {
 };
 static_assert(sizeof(SectorDesc) % 8 == 0, "sector descriptors are staged as 64-bit words");
 
-inline PackedLayout make_packed_layout(const MatvecProblem& p, int n_sectors = 0) {
+// Shared-memory layout of a packed kernel launched with `threads` threads per block.
+inline PackedLayout make_packed_layout(const MatvecProblem& p, int n_sectors, int threads) {
   PackedLayout L{};
   auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
   const size_t Gp = 32 * (size_t)p.group.gpl;
+  const size_t S = (size_t)rec_stride(p.group.gpl);
+  const size_t warps = (size_t)(threads + 31) / 32;
   size_t o = 0;
-  L.off_onehot = o; o = al(o + (size_t)p.group.n_bits * Gp * 8);
+  L.off_rec = o; o = al(o + (size_t)p.group.n_bits * 32 * S * 4);
+  L.off_ga = o; o = al(o + warps * 32 * S * 4);
   L.off_chars = o; o = al(o + (n_sectors > 0 ? 0 : Gp * 16));
   L.off_tm = o; o = al(o + (size_t)p.off.n * 8);
   L.off_tl = o; o = al(o + (size_t)p.off.n * 8);
@@ -439,15 +452,10 @@ inline PackedLayout make_packed_layout(const MatvecProblem& p, int n_sectors = 0
   return L;
 }
 
-__device__ __forceinline__ uint64_t flip_packed(uint64_t cand, uint64_t flipkey) {
-  // top state bit set -> the flipped image is the smaller one; XOR the value bits and the flip bit
-  const uint32_t m = (uint32_t)((int32_t)(uint32_t)(cand >> 32) >> 31);
-  return cand ^ (flipkey & (((uint64_t)m << 32) | m));
-}
-
 // Shared-memory tables of the packed kernels.
 struct PackedTables {
-  const uint64_t* oh;  // one-hot site images [n_bits][gpl * 32]
+  const uint32_t* rec; // site images as lane records [n_bits][32][S]
+  uint32_t* ga;        // per-warp records of g.a [warps][32][S]
   const double2* ch;   // characters (single-sector kernel only)
   const uint64_t *tm, *tl, *tx, *ts;
   const double2* tv;
@@ -458,13 +466,15 @@ struct PackedTables {
   int nt, nd;
 };
 
-// Copies the group's site images, the term tables and (with_chars) the characters into shared
-// memory; the caller synchronises the block afterwards.
+// Copies the group's site images (as lane records), the term tables and (with_chars) the
+// characters into shared memory; the caller synchronises the block afterwards.
 __device__ __forceinline__ PackedTables stage_packed(const MatvecProblem& p, const PackedLayout& L,
                                                      unsigned char* smem, bool with_chars) {
   PackedTables T;
-  const int Gp = 32 * p.group.gpl;
-  uint64_t* oh = (uint64_t*)(smem + L.off_onehot);
+  const int gpl = p.group.gpl;
+  const int Gp = 32 * gpl;
+  const int S = rec_stride(gpl);
+  uint32_t* rec = (uint32_t*)(smem + L.off_rec);
   double2* ch = (double2*)(smem + L.off_chars);
   uint64_t* tm = (uint64_t*)(smem + L.off_tm);
   uint64_t* tl = (uint64_t*)(smem + L.off_tl);
@@ -476,7 +486,14 @@ __device__ __forceinline__ PackedTables stage_packed(const MatvecProblem& p, con
   uint64_t* dr = (uint64_t*)(smem + L.off_dr);
   uint64_t* ds = (uint64_t*)(smem + L.off_ds);
   double2* dv = (double2*)(smem + L.off_dv);
-  stage_u64(oh, p.group.onehot_packed, p.group.n_bits * Gp);
+  const int n_img = p.group.n_bits * Gp;
+  for (int i = threadIdx.x; i < n_img; i += blockDim.x) {
+    const int r = i / Gp, e = i - r * Gp;
+    const uint64_t v = __ldg(p.group.onehot_packed + i);
+    uint32_t* dst = rec + (r * 32 + (e & 31)) * S + 2 * (e >> 5);
+    dst[0] = (uint32_t)v;
+    dst[1] = (uint32_t)(v >> 32);
+  }
   if (with_chars) stage_d2(ch, p.group.chars_packed, Gp);
   stage_u64(tm, p.off.m, p.off.n);
   stage_u64(tl, p.off.l, p.off.n);
@@ -491,11 +508,144 @@ __device__ __forceinline__ PackedTables stage_packed(const MatvecProblem& p, con
   uint64_t* fs = (uint64_t*)(smem + L.off_fsign);
   if (p.group.fermionic) stage_u64(fs, p.group.fsign_packed, p.group.n_bits * Gp);
   T.fs = fs;
-  T.oh = oh; T.ch = ch; T.tm = tm; T.tl = tl; T.tx = tx; T.ts = ts; T.tv = tv; T.ti = ti;
+  T.rec = rec;
+  T.ga = (uint32_t*)(smem + L.off_ga);
+  T.ch = ch; T.tm = tm; T.tl = tl; T.tx = tx; T.ts = ts; T.tv = tv; T.ti = ti;
   T.dm = dm; T.dr = dr; T.ds = ds; T.dv = dv;
   T.nt = p.off.n;
   T.nd = p.diag.n;
   return T;
+}
+
+// Keys of the orbit scan for states of nbits bits (stored in the top bits of a 64-bit word):
+// the state bits of the high word, and the flip key (all state bits and the flip bit of the
+// candidate index) as its two words.
+struct ScanKeys {
+  uint32_t hmask, fk_lo, fk_hi;
+};
+__device__ __forceinline__ ScanKeys scan_keys(int nbits) {
+  const int SH = 64 - nbits;
+  const uint64_t flipkey = ((~0ull >> SH) << SH) | 1ull;
+  return ScanKeys{(uint32_t)(flipkey >> 32), (uint32_t)flipkey, (uint32_t)(flipkey >> 32)};
+}
+
+// g.a for this lane's slots (XOR of the images of a's set bits, two sites at a time), with the
+// candidate index 2 * (lane + 32 k) in the low bits: the high words are returned in gh, both
+// words go to this lane's record of the warp's area gw (read by the tie pass of scan_two_site).
+template <int GPL>
+__device__ __forceinline__ void row_images(const uint32_t* __restrict__ rec, uint32_t* __restrict__ gw, uint64_t a,
+                                           int lane, uint32_t (&gh)[GPL]) {
+  constexpr int S = 2 * GPL + 1;
+  const uint32_t* recl = rec + lane * S;
+  uint32_t gl[GPL];
+#pragma unroll
+  for (int k = 0; k < GPL; ++k) gl[k] = gh[k] = 0u;
+  uint64_t bits = a;
+  while (bits != 0) {
+    const uint32_t* r0 = recl + (__ffsll((long long)bits) - 1) * 32 * S;
+    bits &= bits - 1;
+    if (bits == 0) {
+#pragma unroll
+      for (int k = 0; k < GPL; ++k) {
+        gl[k] ^= r0[2 * k];
+        gh[k] ^= r0[2 * k + 1];
+      }
+      break;
+    }
+    const uint32_t* r1 = recl + (__ffsll((long long)bits) - 1) * 32 * S;
+    bits &= bits - 1;
+#pragma unroll
+    for (int k = 0; k < GPL; ++k) {
+      gl[k] ^= r0[2 * k] ^ r1[2 * k];
+      gh[k] ^= r0[2 * k + 1] ^ r1[2 * k + 1];
+    }
+  }
+  uint32_t* mine = gw + lane * S;
+#pragma unroll
+  for (int k = 0; k < GPL; ++k) {
+    mine[2 * k] = gl[k] | (uint32_t)(2 * (lane + 32 * k));
+    mine[2 * k + 1] = gh[k];
+  }
+  __syncwarp();
+}
+
+// Orbit scan of beta = a ^ (sites s0, s1): the smallest 64-bit key over all slots (and their spin
+// flips), i.e. (representative << SH) | (2 * element + flipped), the same key as a full 64-bit
+// minimum.  Pass 1: per slot the high word h = g.a ^ image(s0) ^ image(s1); with spin inversion
+// the candidate is min(h, flip(h)) and min over slots of that is min(min h, flip(max h)), so one
+// min and one max per slot.  Pass 2: only lanes whose pass-1 minimum ties the warp's take part;
+// for each, lanes j < GPL rebuild the exact key of its slot j and keep the lowest low word among
+// the keys whose high word is the minimum.
+template <int GPL, bool INV>
+__device__ __forceinline__ uint64_t scan_two_site(const uint32_t* __restrict__ rec, const uint32_t* __restrict__ gw,
+                                                  const uint32_t (&gh)[GPL], int s0, int s1, int lane,
+                                                  const ScanKeys& K) {
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int S = 2 * GPL + 1;
+  const uint32_t* p0 = rec + (s0 * 32 + lane) * S + 1;
+  const uint32_t* p1 = rec + (s1 * 32 + lane) * S + 1;
+  uint32_t mn = 0xffffffffu, mx = 0u;
+#pragma unroll
+  for (int k = 0; k < GPL; ++k) {
+    const uint32_t h = gh[k] ^ p0[2 * k] ^ p1[2 * k];
+    mn = min(mn, h);
+    if (INV) mx = max(mx, h);
+  }
+  const uint32_t lm = INV ? min(mn, ~mx & K.hmask) : mn;
+  const uint32_t mhi = __reduce_min_sync(FULL, lm);
+  unsigned M = __ballot_sync(FULL, lm == mhi);
+  const uint32_t* q0 = rec + s0 * 32 * S + 2 * lane;
+  const uint32_t* q1 = rec + s1 * 32 * S + 2 * lane;
+  const uint32_t* qg = gw + 2 * lane;
+  uint32_t blo = 0xffffffffu;
+  do {
+    const int o = (__ffs(M) - 1) * S;
+    M &= M - 1;
+    if (lane < GPL) {
+      uint32_t lo = qg[o] ^ q0[o] ^ q1[o];
+      uint32_t hi = qg[o + 1] ^ q0[o + 1] ^ q1[o + 1];
+      if (INV && (int32_t)hi < 0) {
+        lo ^= K.fk_lo;
+        hi ^= K.fk_hi;
+      }
+      if (hi == mhi) blo = min(blo, lo);
+    }
+  } while (M != 0);
+  const uint32_t mlo = __reduce_min_sync(FULL, blo);
+  return ((uint64_t)mhi << 32) | mlo;
+}
+
+// Orbit scan of beta = a ^ xt for any number of flipped sites: full 64-bit keys per slot.
+template <int GPL, bool INV>
+__device__ __forceinline__ uint64_t scan_general(const uint32_t* __restrict__ rec, const uint32_t* __restrict__ gw,
+                                                 const uint32_t (&gh)[GPL], uint64_t xt, int lane,
+                                                 const ScanKeys& K) {
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int S = 2 * GPL + 1;
+  const uint32_t* recl = rec + lane * S;
+  const uint32_t* mine = gw + lane * S;
+  const uint64_t fk = ((uint64_t)K.fk_hi << 32) | K.fk_lo;
+  uint64_t cand[GPL];
+#pragma unroll
+  for (int k = 0; k < GPL; ++k) {
+    uint32_t lo = mine[2 * k], hi = gh[k];
+    for (uint64_t bits = xt; bits != 0; bits &= bits - 1) {
+      const uint32_t* r = recl + (__ffsll((long long)bits) - 1) * 32 * S + 2 * k;
+      lo ^= r[0];
+      hi ^= r[1];
+    }
+    const uint64_t v = ((uint64_t)hi << 32) | lo;
+    cand[k] = (INV && (int32_t)hi < 0) ? (v ^ fk) : v;
+  }
+#pragma unroll
+  for (int w = 1; w < GPL; w *= 2) {
+#pragma unroll
+    for (int k = 0; k + w < GPL; k += 2 * w) cand[k] = cand[k + w] < cand[k] ? cand[k + w] : cand[k];
+  }
+  const uint32_t hi = (uint32_t)(cand[0] >> 32), lo = (uint32_t)cand[0];
+  const uint32_t mhi = __reduce_min_sync(FULL, hi);
+  const uint32_t mlo = __reduce_min_sync(FULL, hi == mhi ? lo : 0xffffffffu);
+  return ((uint64_t)mhi << 32) | mlo;
 }
 
 // One output row of the packed kernels (executed by a whole warp): y[row, 0..K) for the sector
@@ -527,11 +677,11 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
   const int lane = threadIdx.x & 31;
   const int SH = 64 - nbits;
   const uint64_t lowmask = (1ull << SH) - 1;
-  const uint64_t flipkey = ((~0ull >> SH) << SH) | 1ull;  // all state bits and the flip bit
+  const ScanKeys keys = scan_keys(nbits);
   const int rhs = lane % K;
   const int q = lane / K;
-  const uint64_t* ohl = T.oh + lane;
   const int nt = T.nt;
+  uint32_t* gw = T.ga + (threadIdx.x >> 5) * 32 * rec_stride(GPL);  // this warp's g.a records
 
   const uint64_t a = __ldg(ix.reps + row);
   const double inv_na = __ldg(ix.inv_norms + row);
@@ -545,27 +695,10 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
     }
     return;
   }
-  // g.a for this lane's slots: XOR of the one-hot images of a's set bits, two bits at a time
-  // (one three-input XOR per pair)
-  uint64_t ga[GPL];
-#pragma unroll
-  for (int k = 0; k < GPL; ++k) ga[k] = 0;
-  uint64_t bits = a;
-  while (bits != 0) {
-    const uint64_t* r0 = ohl + (__ffsll((long long)bits) - 1) * Gp;
-    bits &= bits - 1;
-    if (bits == 0) {
-#pragma unroll
-      for (int k = 0; k < GPL; ++k) ga[k] ^= r0[32 * k];
-      break;
-    }
-    const uint64_t* r1 = ohl + (__ffsll((long long)bits) - 1) * Gp;
-    bits &= bits - 1;
-#pragma unroll
-    for (int k = 0; k < GPL; ++k) ga[k] ^= r0[32 * k] ^ r1[32 * k];
-  }
-#pragma unroll
-  for (int k = 0; k < GPL; ++k) ga[k] |= (uint64_t)(2 * (lane + 32 * k));
+  // g.a for this lane's slots (high words here, both words in the warp's records)
+  __syncwarp();  // the previous row's scans have read the records
+  uint32_t gh[GPL];
+  row_images<GPL>(T.rec, gw, a, lane, gh);
 
   double dre = 0.0, dim = 0.0;
   F2 dpr{0.0f, 0.0f}, dpi{0.0f, 0.0f};  // PAIR: the diagonal element as pairs
@@ -730,36 +863,12 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
           continue;
         }
       }
-      uint64_t cand[GPL];
-      if (((info >> 16) & 0xffu) == 2u) {
-        const uint64_t* r0 = ohl + (int)(info & 0xffu) * Gp;
-        const uint64_t* r1 = ohl + (int)((info >> 8) & 0xffu) * Gp;
-#pragma unroll
-        for (int k = 0; k < GPL; ++k) {
-          cand[k] = ga[k] ^ r0[32 * k] ^ r1[32 * k];
-          if (INV) cand[k] = flip_packed(cand[k], flipkey);
-        }
-      } else {
-#pragma unroll
-        for (int k = 0; k < GPL; ++k) {
-          uint64_t v = ga[k];
-          for (uint64_t bits = xt; bits != 0; bits &= bits - 1)
-            v ^= ohl[(__ffsll((long long)bits) - 1) * Gp + 32 * k];
-          cand[k] = INV ? flip_packed(v, flipkey) : v;
-        }
-      }
-      // pairwise (tree) minimum: short dependency chains
-#pragma unroll
-      for (int w = 1; w < GPL; w *= 2) {
-#pragma unroll
-        for (int k = 0; k + w < GPL; k += 2 * w) cand[k] = cand[k + w] < cand[k] ? cand[k + w] : cand[k];
-      }
-      const uint64_t best = cand[0];
-      const uint32_t hi = (uint32_t)(best >> 32), lo = (uint32_t)best;
-      const uint32_t mhi = __reduce_min_sync(FULL, hi);
-      const uint32_t mlo = __reduce_min_sync(FULL, hi == mhi ? lo : 0xffffffffu);
+      const uint64_t key = (((info >> 16) & 0xffu) == 2u)
+                               ? scan_two_site<GPL, INV>(T.rec, gw, gh, (int)(info & 0xffu),
+                                                         (int)((info >> 8) & 0xffu), lane, keys)
+                               : scan_general<GPL, INV>(T.rec, gw, gh, xt, lane, keys);
       if (lane == nslot) {
-        my_key = ((uint64_t)mhi << 32) | mlo;
+        my_key = key;
         my_t = t;
       }
       if (++nslot == 32) {
@@ -820,10 +929,18 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
   }
 }
 
-// Pair kernels on small groups hold few registers: three CTAs per SM (more warps to hide the
-// gathers' latency).
+// Launch bounds of the packed single-sector kernels.  The one-vector kernels run CTAs of up to
+// 768 threads (at most 85 registers per thread): one CTA per SM, whose 24 warps share one copy
+// of the tables; multi-column FP64 kernels up to 640 threads (102 registers); the pair kernels
+// keep 320-thread CTAs, three per SM on small groups (more warps to hide the gathers' latency).
+template <int GPL, int K, bool PAIR>
+struct PackedBounds {
+  static constexpr int threads = PAIR ? 320 : (K == 1 ? 768 : 640);
+  static constexpr int min_blocks = PAIR ? ((GPL <= 2) ? 3 : 2) : 1;
+};
+
 template <int GPL, bool INV, bool CPLX, int K, bool FERMI = false, bool PAIR = false>
-__global__ void __launch_bounds__(320, (PAIR && GPL <= 2) ? 3 : 2)
+__global__ void __launch_bounds__(PackedBounds<GPL, K, PAIR>::threads, PackedBounds<GPL, K, PAIR>::min_blocks)
     k_matvec_packed(const MatvecProblem p, const PackedLayout L, const double* __restrict__ x, int64_t ldx,
                     double* __restrict__ y, int64_t ldy, int* __restrict__ err,
                     const uint64_t* __restrict__ binom) {

@@ -35,19 +35,33 @@ static int launch_with_smem(Kernel kern, const char* name, const MatvecProblem& 
   return cuda_ok(cudaGetLastError(), name) ? 0 : LS_GPU_ERR_CUDA;
 }
 
+// Launches the packed single-sector kernel `kern` (compiled for at most max_threads threads per
+// CTA) with the shape and shared-memory layout that packed_launch_shape picks.
+template <typename Kernel>
+static int launch_packed_kernel(Kernel kern, int max_threads, const char* name, const MatvecProblem& p,
+                                const double* x, int64_t ldx, double* y, int64_t ldy, int* err,
+                                const uint64_t* binom, cudaStream_t s) {
+  LaunchShape sh{};
+  PackedLayout L{};
+  const int rc = packed_launch_shape((const void*)kern, max_threads, p, 0, p.n_rows, &sh, &L);
+  if (rc != 0) return rc;
+  kern<<<sh.blocks, sh.threads, L.total, s>>>(p, L, x, ldx, y, ldy, err, binom);
+  return cuda_ok(cudaGetLastError(), name) ? 0 : LS_GPU_ERR_CUDA;
+}
+
 }  // namespace lsg
 
 // Defines NAME(gpl, inv, ...) launching k_matvec_packed<GPL, INV, CPLX, K>.
 #define LSG_DEFINE_PACKED(NAME, CPLX, K)                                                          \
-  int NAME(int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L, LaunchShape sh,      \
-           const double* x, int64_t ldx, double* y, int64_t ldy, int* err, const uint64_t* binom, \
-           cudaStream_t s) {                                                                      \
+  int NAME(int gpl, bool inv, const MatvecProblem& p, const double* x, int64_t ldx, double* y,    \
+           int64_t ldy, int* err, const uint64_t* binom, cudaStream_t s) {                        \
     auto run = [&](auto gtag) -> int {                                                            \
       constexpr int G = decltype(gtag)::value;                                                    \
-      return inv ? launch_with_smem(k_matvec_packed<G, true, CPLX, K>, #NAME, p, L, sh, x, ldx, y, \
-                                    ldy, err, binom, s)                                          \
-                 : launch_with_smem(k_matvec_packed<G, false, CPLX, K>, #NAME, p, L, sh, x, ldx,  \
-                                    y, ldy, err, binom, s);                                      \
+      constexpr int MT = PackedBounds<G, K, false>::threads;                                      \
+      return inv ? launch_packed_kernel(k_matvec_packed<G, true, CPLX, K>, MT, #NAME, p, x, ldx,  \
+                                        y, ldy, err, binom, s)                                   \
+                 : launch_packed_kernel(k_matvec_packed<G, false, CPLX, K>, MT, #NAME, p, x, ldx, \
+                                        y, ldy, err, binom, s);                                  \
     };                                                                                            \
     switch (gpl) {                                                                                \
       case 1: return run(std::integral_constant<int, 1>{});                                       \
@@ -64,15 +78,15 @@ static int launch_with_smem(Kernel kern, const char* name, const MatvecProblem& 
 
 // Defines NAME(gpl, inv, ...) launching the FP32-pair k_matvec_packed<GPL, INV, true, K, false, true>.
 #define LSG_DEFINE_PACKED_PAIR(NAME, K)                                                           \
-  int NAME(int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L, LaunchShape sh,      \
-           const double* x, int64_t ldx, double* y, int64_t ldy, int* err, const uint64_t* binom, \
-           cudaStream_t s) {                                                                      \
+  int NAME(int gpl, bool inv, const MatvecProblem& p, const double* x, int64_t ldx, double* y,    \
+           int64_t ldy, int* err, const uint64_t* binom, cudaStream_t s) {                        \
     auto run = [&](auto gtag) -> int {                                                            \
       constexpr int G = decltype(gtag)::value;                                                    \
-      return inv ? launch_with_smem(k_matvec_packed<G, true, true, K, false, true>, #NAME, p, L, sh, \
-                                    x, ldx, y, ldy, err, binom, s)                               \
-                 : launch_with_smem(k_matvec_packed<G, false, true, K, false, true>, #NAME, p, L,  \
-                                    sh, x, ldx, y, ldy, err, binom, s);                          \
+      constexpr int MT = PackedBounds<G, K, true>::threads;                                       \
+      return inv ? launch_packed_kernel(k_matvec_packed<G, true, true, K, false, true>, MT, #NAME, \
+                                        p, x, ldx, y, ldy, err, binom, s)                        \
+                 : launch_packed_kernel(k_matvec_packed<G, false, true, K, false, true>, MT,       \
+                                        #NAME, p, x, ldx, y, ldy, err, binom, s);                \
     };                                                                                            \
     switch (gpl) {                                                                                \
       case 1: return run(std::integral_constant<int, 1>{});                                       \

@@ -9,19 +9,20 @@ namespace lsg {
 LSG_DECLARE_PACKED(launch_packed_pair_k8)
 LSG_DECLARE_PACKED(launch_packed_pair_k16)
 
-int launch_packed_pair(int k, int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L, LaunchShape sh,
-                       const double* x, int64_t ldx, double* y, int64_t ldy, int* err, const uint64_t* binom,
-                       cudaStream_t s) {
+int launch_packed_pair(int k, int gpl, bool inv, const MatvecProblem& p, const double* x, int64_t ldx, double* y,
+                       int64_t ldy, int* err, const uint64_t* binom, cudaStream_t s) {
   if (p.xs == nullptr) return fail(LS_GPU_ERR_INVALID, "pair kernels gather from a prescaled pair copy of x");
   if (p.group.fermionic) {
     if (inv) return fail(LS_GPU_ERR_INVALID, "fermionic groups have no spin inversion");
     auto with_k = [&](auto gtag) -> int {
       constexpr int G = decltype(gtag)::value;
       switch (k) {
-        case 8: return launch_with_smem(k_matvec_packed<G, false, true, 8, true, true>, "k_matvec_packed<fermi,pair>",
-                                        p, L, sh, x, ldx, y, ldy, err, binom, s);
-        case 16: return launch_with_smem(k_matvec_packed<G, false, true, 16, true, true>,
-                                         "k_matvec_packed<fermi,pair>", p, L, sh, x, ldx, y, ldy, err, binom, s);
+        case 8: return launch_packed_kernel(k_matvec_packed<G, false, true, 8, true, true>,
+                                            PackedBounds<G, 8, true>::threads, "k_matvec_packed<fermi,pair>", p, x,
+                                            ldx, y, ldy, err, binom, s);
+        case 16: return launch_packed_kernel(k_matvec_packed<G, false, true, 16, true, true>,
+                                             PackedBounds<G, 16, true>::threads, "k_matvec_packed<fermi,pair>", p, x,
+                                             ldx, y, ldy, err, binom, s);
         default: return LS_GPU_ERR_INVALID;
       }
     };
@@ -34,19 +35,22 @@ int launch_packed_pair(int k, int gpl, bool inv, const MatvecProblem& p, const P
     }
   }
   switch (k) {
-    case 8: return launch_packed_pair_k8(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
-    case 16: return launch_packed_pair_k16(gpl, inv, p, L, sh, x, ldx, y, ldy, err, binom, s);
+    case 8: return launch_packed_pair_k8(gpl, inv, p, x, ldx, y, ldy, err, binom, s);
+    case 16: return launch_packed_pair_k16(gpl, inv, p, x, ldx, y, ldy, err, binom, s);
     default: return LS_GPU_ERR_INVALID;
   }
 }
 
-int launch_sectors_pair(int k, int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L, LaunchShape sh,
+int launch_sectors_pair(int k, int gpl, bool inv, const MatvecProblem& p, int n_sectors_layout,
                         const SectorDesc* d_desc, int n_sectors, int64_t total_rows, int64_t ldx, int64_t ldy,
                         int* err, const uint64_t* binom, const double* xs_all, int64_t ldxs, int col,
                         cudaStream_t s) {
   if (xs_all == nullptr) return fail(LS_GPU_ERR_INVALID, "pair kernels gather from a prescaled pair copy of x");
   auto go = [&](auto kern) -> int {
-    if (!ensure_smem_limit((const void*)kern, L.total)) return LS_GPU_ERR_CUDA;
+    LaunchShape sh{};
+    PackedLayout L{};
+    const int rc = packed_launch_shape((const void*)kern, 320, p, n_sectors_layout, total_rows, &sh, &L);
+    if (rc != 0) return rc;
     kern<<<sh.blocks, sh.threads, L.total, s>>>(p, L, d_desc, n_sectors, total_rows, ldx, ldy, err, binom, xs_all,
                                                 ldxs, col);
     return cuda_ok(cudaGetLastError(), "k_matvec_sectors<pair>") ? 0 : LS_GPU_ERR_CUDA;

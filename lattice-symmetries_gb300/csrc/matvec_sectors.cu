@@ -7,11 +7,14 @@
 
 namespace lsg {
 
-int launch_sectors(int k, int gpl, bool inv, const MatvecProblem& p, const PackedLayout& L, LaunchShape sh,
-                   const SectorDesc* d_desc, int n_sectors, int64_t total_rows, int64_t ldx, int64_t ldy,
-                   int* err, const uint64_t* binom, const double* xs_all, int64_t ldxs, int col, cudaStream_t s) {
+int launch_sectors(int k, int gpl, bool inv, const MatvecProblem& p, int n_sectors_layout, const SectorDesc* d_desc,
+                   int n_sectors, int64_t total_rows, int64_t ldx, int64_t ldy, int* err, const uint64_t* binom,
+                   const double* xs_all, int64_t ldxs, int col, cudaStream_t s) {
   auto go = [&](auto kern) -> int {
-    if (!ensure_smem_limit((const void*)kern, L.total)) return LS_GPU_ERR_CUDA;
+    LaunchShape sh{};
+    PackedLayout L{};
+    const int rc = packed_launch_shape((const void*)kern, 320, p, n_sectors_layout, total_rows, &sh, &L);
+    if (rc != 0) return rc;
     kern<<<sh.blocks, sh.threads, L.total, s>>>(p, L, d_desc, n_sectors, total_rows, ldx, ldy, err, binom, xs_all,
                                                 ldxs, col);
     return cuda_ok(cudaGetLastError(), "k_matvec_sectors") ? 0 : LS_GPU_ERR_CUDA;
