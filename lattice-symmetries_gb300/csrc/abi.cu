@@ -1042,7 +1042,7 @@ int upload_terms(const TermTable& t, const DeviceConstraint& cons, DeviceTermSet
     uint32_t info = (uint32_t)lo | ((uint32_t)hi << 8) | ((uint32_t)cnt << 16);
     if (term_breaks_constraint(cons, t.l[k], t.r[k])) info |= kTermNeedsCheck;
     xinfo[k] = info;
-    if (cnt != 2) all_two = 0;
+    if (cnt != 2 || (info & kTermNeedsCheck)) all_two = 0;
   }
   put(xinfo.data(), t.n * 4, oi);
   out->terms.all_two_site = all_two;

@@ -105,7 +105,8 @@ struct DeviceTerms {
   // Per term: bits 0-7 lowest flipped site, 8-15 highest flipped site, 16-23 number of flipped
   // sites, bit 24 set when the term can change a conserved particle number of the basis.
   const uint32_t* xinfo = nullptr;
-  int all_two_site = 0;               // every term flips exactly two sites
+  int all_two_site = 0;               // every term flips exactly two sites and keeps the basis'
+                                      // conserved numbers (no term needs a constraint check)
 };
 constexpr uint32_t kTermNeedsCheck = 1u << 24;
 

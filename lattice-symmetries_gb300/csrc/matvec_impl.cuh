@@ -464,6 +464,7 @@ struct PackedTables {
   const double2* dv;
   const uint64_t* fs;  // fermionic sign tables (fermionic groups)
   int nt, nd;
+  int all2;            // every off-diagonal term flips two sites and needs no constraint check
 };
 
 // Copies the group's site images (as lane records), the term tables and (with_chars) the
@@ -514,6 +515,7 @@ __device__ __forceinline__ PackedTables stage_packed(const MatvecProblem& p, con
   T.dm = dm; T.dr = dr; T.ds = ds; T.dv = dv;
   T.nt = p.off.n;
   T.nd = p.diag.n;
+  T.all2 = p.off.all_two_site;
   return T;
 }
 
@@ -594,22 +596,23 @@ __device__ __forceinline__ uint64_t scan_two_site(const uint32_t* __restrict__ r
   const uint32_t lm = INV ? min(mn, ~mx & K.hmask) : mn;
   const uint32_t mhi = __reduce_min_sync(FULL, lm);
   unsigned M = __ballot_sync(FULL, lm == mhi);
-  const uint32_t* q0 = rec + s0 * 32 * S + 2 * lane;
-  const uint32_t* q1 = rec + s1 * 32 * S + 2 * lane;
-  const uint32_t* qg = gw + 2 * lane;
+  // lanes beyond the slots repeat the last slot (same candidate): no divergent branch
+  const int jj = lane < GPL ? lane : GPL - 1;
+  const uint32_t* q0 = rec + s0 * 32 * S + 2 * jj;
+  const uint32_t* q1 = rec + s1 * 32 * S + 2 * jj;
+  const uint32_t* qg = gw + 2 * jj;
   uint32_t blo = 0xffffffffu;
   do {
     const int o = (__ffs(M) - 1) * S;
     M &= M - 1;
-    if (lane < GPL) {
-      uint32_t lo = qg[o] ^ q0[o] ^ q1[o];
-      uint32_t hi = qg[o + 1] ^ q0[o + 1] ^ q1[o + 1];
-      if (INV && (int32_t)hi < 0) {
-        lo ^= K.fk_lo;
-        hi ^= K.fk_hi;
-      }
-      if (hi == mhi) blo = min(blo, lo);
+    uint32_t lo = qg[o] ^ q0[o] ^ q1[o];
+    uint32_t hi = qg[o + 1] ^ q0[o + 1] ^ q1[o + 1];
+    if (INV) {  // flip when the top state bit is set: all-ones mask from the sign bit
+      const uint32_t f = (uint32_t)((int32_t)hi >> 31);
+      lo ^= K.fk_lo & f;
+      hi ^= K.fk_hi & f;
     }
+    blo = (hi == mhi) ? min(blo, lo) : blo;
   } while (M != 0);
   const uint32_t mlo = __reduce_min_sync(FULL, blo);
   return ((uint64_t)mhi << 32) | mlo;
@@ -848,7 +851,35 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
     }
   };
 
-  for (int t0 = 0; t0 < nt; t0 += 32) {
+  if (T.all2) {
+    // Every term flips two sites and keeps the conserved numbers (warp-uniform): batches of up
+    // to 32 elements are scanned in a tight loop, each batch then flushed.
+    int t0 = 0;
+    unsigned mask = __ballot_sync(FULL, lane < nt && (a & T.tm[lane]) == T.tl[lane]);
+    for (;;) {
+      nslot = 0;
+      while (nslot < 32) {
+        while (mask == 0 && t0 + 32 < nt) {
+          t0 += 32;
+          const int tt = t0 + lane;
+          mask = __ballot_sync(FULL, tt < nt && (a & T.tm[tt]) == T.tl[tt]);
+        }
+        if (mask == 0) break;
+        const int t = t0 + __ffs(mask) - 1;
+        mask &= mask - 1;
+        const uint32_t info = T.ti[t];
+        const uint64_t key = scan_two_site<GPL, INV>(T.rec, gw, gh, (int)(info & 0xffu), (int)((info >> 8) & 0xffu),
+                                                     lane, keys);
+        my_key = lane == nslot ? key : my_key;
+        my_t = lane == nslot ? t : my_t;
+        ++nslot;
+      }
+      if (nslot > 0) flush();
+      if (nslot < 32) break;
+    }
+    nslot = 0;
+  }
+  for (int t0 = 0; !T.all2 && t0 < nt; t0 += 32) {
     const int tt = t0 + lane;
     const bool hit = tt < nt && (a & T.tm[tt]) == T.tl[tt];
     unsigned mask = __ballot_sync(FULL, hit);
