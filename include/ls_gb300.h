@@ -428,9 +428,10 @@ int ls_gpu_state_index(ls_hs_basis const *basis, int64_t batch, uint64_t const *
 int ls_gpu_enumerate_noalloc(ls_hs_basis const *basis, uint64_t *d_out, int64_t capacity,
                              int64_t *count, void *stream);
 
-/* Tuning knobs of the projected matvec kernels: threads per CTA (a multiple of 32, at most 768;
- * 0 = each kernel's own maximum: 768 for one right-hand side, 640 for FP64 blocks, 320 for the
- * FP32-pair and batched kernels, lowered until the shared-memory tables fit) and grid waves (the
+/* Tuning knobs of the projected matvec kernels: threads per CTA (a multiple of 32, at most 1024;
+ * 0 = each kernel's own maximum: 1024 for one right-hand side (768 for groups of more than 288
+ * elements), 640 for FP64 blocks, 320 for the FP32-pair and batched kernels, lowered until the
+ * shared-memory tables fit) and grid waves (the
  * grid is SMs x resident CTAs per SM x waves, one warp per row at a time; 0 = 1).  The fallback
  * kernel for groups whose packed tables do not fit (or 64-bit states) always runs 256-thread
  * CTAs. */
@@ -451,7 +452,7 @@ int ls_gpu_get_block_arithmetic(void);
 int ls_gpu_set_matvec_rhs_tile(int rhs_tile);
 int ls_gpu_get_matvec_config(int *threads_per_block, int *waves, int *rhs_tile);
 /* Autotuner: times the matvec of `op` on k complex right-hand sides over a table of
- * (threads, waves) pairs ({kernel maximum, 320, 512} x {1, 2, 4}) and, for k >= 8,
+ * (threads, waves) pairs ({kernel maximum, 768, 512} x {1, 2, 4}) and, for k >= 8,
  * right-hand-side tiles, and installs the fastest; reports the launch shape (threads 0 = the
  * kernel maximum) and its time (ms). */
 int ls_gpu_autotune_matvec(ls_hs_operator const *op, int k, int *best_threads, int *best_waves,

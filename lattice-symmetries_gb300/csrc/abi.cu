@@ -1284,7 +1284,7 @@ extern "C" int ls_gpu_autotune_matvec(ls_hs_operator const* op, int k, int* best
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   // threads per CTA (each kernel clamps to its own maximum; 0 = that maximum) x grid waves
-  const int threads_choices[] = {0, 320, 512};
+  const int threads_choices[] = {0, 768, 512};
   const int wave_choices[] = {1, 2, 4};
   double best = 1e300;
   int bt = 0, bw = 1, rc = 0;

@@ -35,9 +35,9 @@ static int g_blocks_per_sm_override = 0;
 static int g_rhs_tile = 16;  // most right-hand sides per launch (16, 8, 4 or 1)
 
 int set_matvec_config(int threads, int blocks_per_sm) {
-  // the warp-per-row kernels are compiled for at most 768 threads per block (each kernel clamps
+  // the warp-per-row kernels are compiled for at most 1024 threads per block (each kernel clamps
   // the setting to its own maximum)
-  if (threads != 0 && (threads < 32 || threads > 768 || threads % 32 != 0)) return LS_GPU_ERR_INVALID;
+  if (threads != 0 && (threads < 32 || threads > 1024 || threads % 32 != 0)) return LS_GPU_ERR_INVALID;
   if (blocks_per_sm < 0 || blocks_per_sm > 64) return LS_GPU_ERR_INVALID;
   g_threads_override = threads;
   g_blocks_per_sm_override = blocks_per_sm;

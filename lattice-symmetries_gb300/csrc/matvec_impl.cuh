@@ -961,12 +961,13 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
 }
 
 // Launch bounds of the packed single-sector kernels.  The one-vector kernels run CTAs of up to
-// 768 threads (at most 85 registers per thread): one CTA per SM, whose 24 warps share one copy
-// of the tables; multi-column FP64 kernels up to 640 threads (102 registers); the pair kernels
-// keep 320-thread CTAs, three per SM on small groups (more warps to hide the gathers' latency).
+// 1024 threads (at most 64 registers per thread; 768 threads and 85 registers for groups of more
+// than 288 elements): one CTA per SM, whose 32 warps share one copy of the tables; multi-column
+// FP64 kernels up to 640 threads (102 registers); the pair kernels keep 320-thread CTAs, three
+// per SM on small groups (more warps to hide the gathers' latency).
 template <int GPL, int K, bool PAIR>
 struct PackedBounds {
-  static constexpr int threads = PAIR ? 320 : (K == 1 ? 768 : 640);
+  static constexpr int threads = PAIR ? 320 : (K == 1 ? (GPL <= 9 ? 1024 : 768) : 640);
   static constexpr int min_blocks = PAIR ? ((GPL <= 2) ? 3 : 2) : 1;
 };
 

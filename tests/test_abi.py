@@ -197,7 +197,7 @@ def test_host_side_settings_without_a_gpu():
     assert lib.ls_gpu_set_block_arithmetic(3) == -1
     assert ls_.Operator.block_arithmetic() == "auto"
     assert lib.ls_gpu_set_matvec_config(33, 0) == -1
-    assert lib.ls_gpu_set_matvec_config(800, 0) == -1
+    assert lib.ls_gpu_set_matvec_config(1056, 0) == -1
     assert lib.ls_gpu_set_matvec_config(0, 65) == -1
     assert lib.ls_gpu_block_gram(1, 10, 17, None, None, None, None) == -1
     assert b"k <= 16" in lib.ls_gpu_last_error()
