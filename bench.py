@@ -573,25 +573,34 @@ def run_sectors(args):
     ls = importlib.import_module("lattice-symmetries_gb300")
     lat = importlib.import_module("lattice-symmetries_gb300.lattices")
     lanczos = importlib.import_module("lattice-symmetries_gb300.lanczos")
+    rep = importlib.import_module("lattice-symmetries_gb300.replicas")
     c = CONFIGS[args.config]
     n, k = c["n"], c["rhs"]
     expr = lat.xxz(lat.chain_bonds(n), 1.0, c["delta"])
-    torch.cuda.set_device(0)
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    # the sectors (momentum, z): under torchrun each rank takes its share (largest first to the
+    # least loaded rank; the 2n sectors hold about C(n, n/2) / 2n states each, so unit weights)
+    sectors = [(mom, z) for mom in range(n) for z in (1, -1)]
+    mine = rep.my_units([1.0] * len(sectors))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     ops = []
-    for mom in range(n):
-        for z in (1, -1):
-            basis = ls.SpinBasis(n, n // 2, z, ls.Symmetries(lat.chain_symmetries(n, mom)))
-            basis.build(exact_norms=True)
-            ops.append(ls.Operator(basis, expr))
+    for si in mine:
+        mom, z = sectors[si]
+        basis = ls.SpinBasis(n, n // 2, z, ls.Symmetries(lat.chain_symmetries(n, mom)))
+        basis.build(exact_norms=True)
+        ops.append(ls.Operator(basis, expr))
     t_build = time.perf_counter() - t0
     sizes = [op.basis.number_states for op in ops]
     nnzs = [op.count_nonzeros() for op in ops]
-    elements = sum(sizes) + sum(nnzs)  # per right-hand side
+    elements = sum(sizes) + sum(nnzs)  # per right-hand side, this rank's sectors
     batch = ls.SectorBatch(ops, k=k)
-    rng = np.random.default_rng(c["seed"])
     for s, d in enumerate(sizes):
+        rng = np.random.default_rng([c["seed"], mine[s]])  # per-sector stream: same X for any split
         xs = rng.normal(size=(d, k)) + 1j * rng.normal(size=(d, k))
         batch.X[s, :d].copy_(torch.from_numpy(xs))
     # the plan's autotuner: one persistent launch over all sectors, or one launch per sector
@@ -606,15 +615,38 @@ def run_sectors(args):
         batch.replay()
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(0) as clocks:
+    rep.barrier()
+    with ClockSampler(local) as clocks:
         start.record(stream)
         for _ in range(args.steps):
             batch.replay()
         end.record(stream)
         torch.cuda.synchronize()
+    rep.barrier()
     batch.check_errors()
-    t_ms = start.elapsed_time(end) / args.steps
-    value = elements * k / (t_ms * 1e-3)
+    t_ms = rep.max_over_ranks(start.elapsed_time(end) / args.steps)  # the slowest rank
+    elements_all = rep.sum_over_ranks(elements)
+    value = elements_all * k / (t_ms * 1e-3)
+
+    if world > 1:
+        # every rank's sector ground states (block Lanczos on its own batch), merged
+        e0 = lanczos.sector_ground_states(batch, steps=c["lanczos_steps"], seed=c["seed"], graph=True)
+        merged = rep.gather_results({si: float(e) for si, e in zip(mine, e0)})
+        states_all = int(rep.sum_over_ranks(sum(sizes)))
+        if rank == 0:
+            g = min(merged, key=merged.get)
+            print(json.dumps({
+                "metric": "H*x matrix elements/s", "value": value, "unit": "elements/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms, "higher_is_better": True,
+                "scaling": "strong", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+                "config": {"workload": args.config, "description": c["description"], "sectors": len(sectors),
+                           "states": states_all, "rhs": k, "parallelism": "sectors split over {} ranks".format(world),
+                           "block_arithmetic": args.block_arithmetic},
+                "gpu_launches": None, "clocks": clocks.summary(),
+                "extra": {"ground_state_energy": merged[g], "sector_of_ground_state": list(sectors[g]),
+                          "sectors_per_rank": len(mine)}}))
+        torch.distributed.destroy_process_group()
+        return 0
 
     if args.no_extras:
         print(json.dumps({"metric": "H*x matrix elements/s", "value": value, "unit": "elements/s", "n_gpus": 1,
@@ -623,8 +655,12 @@ def run_sectors(args):
                                      "nnz": sum(nnzs), "rhs": k, "form": "batched" if tune["batched"] else
                                      "per-sector launches"}, "gpu_launches": launches_per_run * args.steps}))
         return 0
-    # the same launch with FP64 multiply-adds instead of FP32 pairs, and the difference it makes
-    ls.Operator.block_arithmetic("fp64")
+    # the same launch in the other block arithmetic (FP32 pairs when the headline is FP64, else
+    # FP64), and the difference it makes; the headline number is the --block-arithmetic one
+    other = "auto" if args.block_arithmetic == "fp64" else "fp64"
+    batch.run(check=True)
+    y_head = batch.Y.clone()
+    ls.Operator.block_arithmetic(other)
     batch.run()
     torch.cuda.synchronize()
     start.record(stream)
@@ -632,12 +668,11 @@ def run_sectors(args):
         batch.run()
     end.record(stream)
     torch.cuda.synchronize()
-    t_fp64_block = start.elapsed_time(end) / 2
-    y_fp64 = batch.Y.clone()
+    t_other_block = start.elapsed_time(end) / 2
+    other_rel_l2 = float(torch.linalg.vector_norm(batch.Y - y_head) / torch.linalg.vector_norm(y_head))
     ls.Operator.block_arithmetic(args.block_arithmetic)
     batch.run(check=True)
-    pair_rel_l2 = float(torch.linalg.vector_norm(batch.Y - y_fp64) / torch.linalg.vector_norm(y_fp64))
-    del y_fp64
+    del y_head
     # the same work as one launch per sector (no batching across sectors, no graph)
     start.record(stream)
     for s, op in enumerate(ops):
@@ -724,8 +759,12 @@ def run_sectors(args):
         "extra": {"form": "one persistent launch over all sectors" if tune["batched"] else
                   "one launch per sector (in the CUDA graph)",
                   "autotune_ms": {"batched": tune["ms_batched"], "per_sector": tune["ms_per_sector"]},
-                  "block_arithmetic": args.block_arithmetic, "fp64_block_arithmetic_ms": t_fp64_block,
-                  "pairs_vs_fp64_rel_l2": pair_rel_l2,
+                  "block_arithmetic": args.block_arithmetic,
+                  "other_block_arithmetic": {
+                      "arithmetic": other, "ms_per_step": t_other_block, "rel_l2_vs_headline": other_rel_l2,
+                      "note": "auto = FP32-pair multiply-adds for groups of at most 64 elements (each product "
+                              "below 2^-45 relative, each output within ~2^-45 of the sum of its terms' "
+                              "magnitudes); fp64 = FP64 multiply-adds"},
                   "per_sector_launches_ms": t_loop, "batched_speedup_vs_per_sector": t_loop / t_ms,
                   "plain_one_vector_all_sectors_ms": t_plain,
                   "speedup_per_vector_vs_plain": t_plain * k / t_ms,
@@ -797,24 +836,24 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the block-16 and adjoint lines")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
-    ap.add_argument("--block-arithmetic", default="auto", choices=["auto", "pairs", "fp64"],
-                    help="multiply-adds of complex blocks of 8/16 columns (auto: FP32 pairs for groups of "
-                         "at most 64 elements)")
+    ap.add_argument("--block-arithmetic", default="fp64", choices=["fp64", "auto", "pairs"],
+                    help="multiply-adds of complex blocks of 8/16 columns (fp64, the default; auto: FP32 "
+                         "pairs for groups of at most 64 elements; pairs: FP32 pairs for every group)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
     importlib.import_module("lattice-symmetries_gb300").Operator.block_arithmetic(args.block_arithmetic)
-    if args.config in ("xxz24_sectors", "xxz28_sectors", "hubbard16", "ladder28_grad"):
+    if args.config in ("xxz24_sectors", "xxz28_sectors"):
+        return run_sectors(args)  # under torchrun the sectors are split over the ranks
+    if args.config in ("hubbard16", "ladder28_grad"):
         world, rank, _ = dist_setup()
         if rank != 0:
-            return 0  # single-GPU workloads: under torchrun only rank 0 runs them
+            return 0  # single-sector workloads: under torchrun only rank 0 runs them
         if args.config == "hubbard16":
             return run_hubbard(args)
-        if args.config == "ladder28_grad":
-            return run_ladder(args)
-        return run_sectors(args)
+        return run_ladder(args)
 
     import torch
 
@@ -832,6 +871,12 @@ def main():
     basis.build()
     t_build = time.perf_counter() - t0
     op = ls.Operator(basis, expr)
+    # per-stage times of a second, traced build of the same basis (outside every timed region)
+    ls.stage_times(reset=True)
+    ls.set_tracing(True)
+    build_workload(ls, lat, args.config)[0].build()
+    ls.set_tracing(False)
+    stages_build = ls.stage_times(reset=True)
     D = basis.number_states
     nnz = op.count_nonzeros()
     elements = D + nnz
@@ -861,6 +906,11 @@ def main():
     op.check_errors(sptr)
     t_ms = start.elapsed_time(end)
     t_ms = rep.max_over_ranks(t_ms)  # replicas: the slowest rank's time
+    # per-stage times of one traced step (outside the timed region)
+    ls.set_tracing(True)
+    step()
+    ls.set_tracing(False)
+    stages_step = ls.stage_times(reset=True)
     ms_per_step = t_ms / args.steps
     value = world * elements * args.steps / (t_ms * 1e-3)
 
@@ -929,6 +979,9 @@ def main():
             "nnz": nnz,
             "cpu_baseline": cpu, "parity": parity, "e2e": e2e, "gpu_launches": 2 * args.steps,
             "clocks": clocks.summary(), "basis_build_s": t_build, "extra": extra,
+            "stages_ms": {"basis_build": {k: v[1] for k, v in stages_build.items()},
+                          "matvec_step": {k: v[1] for k, v in stages_step.items()},
+                          "how": "CUDA events per stage (ls_gpu_set_tracing), untimed passes"},
             "autotune": {"threads": tuned[0], "waves": tuned[1], "ms": tuned[2]},
         }
         print(json.dumps(line))

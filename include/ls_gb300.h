@@ -204,7 +204,15 @@ void ls_internal_destroy_halide_kernel_data(void *data);
 
 /* Orbit-scan kernels, FunPtr-compatible: replace ls_hs_is_representative_halide_kernel
  * (kernels.c:195-244) and ls_hs_state_info_halide_kernel (kernels.c:246-319), bound at
- * Basis.hs:921-925.  Host pointers, any strides. */
+ * Basis.hs:921-925.  Host pointers, any strides.
+ *
+ * Lane order: where several group elements map a state to its representative, the character
+ * returned is the one the reference's Halide kernel picks, which depends on the lane width its
+ * build vectorised with (generator.cpp:80, :155-164).  These kernels reproduce the x86-64 AVX2
+ * build the reference ships (kernels/Makefile:21-28): 8 lanes for state_info and 4 for
+ * is_representative (whose floating stabiliser sum is added in the same lane order).  A
+ * reference built for another vector width can return a different (equally valid) character for
+ * such states, and a different rounding residue of that sum. */
 void ls_hs_is_representative_halide_kernel(ptrdiff_t batch_size, uint64_t const *alphas,
                                            ptrdiff_t alphas_stride, uint8_t *are_representatives,
                                            double *norms, void const *private_data);
@@ -309,6 +317,16 @@ int ls_gpu_matvec_f64(ls_hs_operator const *op, int k, double const *d_x, int64_
 int ls_gpu_check_errors(void *stream);
 /* Number of off-diagonal matrix elements (generated targets found in the basis) of H. */
 int ls_gpu_count_nonzeros(ls_hs_operator const *op, int64_t *nnz);
+/* Per-stage timing, off by default (the counterpart of the reference's timing tree,
+ * chapel/src/Utils.chpl:49-144): when on, the library's stages -- basis.enumerate,
+ * basis.enumerate_compact, basis.index, basis.orbit_norms, matvec.prescale, matvec.kernel,
+ * sectors.prescale, sectors.kernel, couplings.kernel, lanczos.gram, lanczos.update -- each open an
+ * NVTX range and record a CUDA-event pair on their stream (no added synchronisation).  Do not
+ * switch it on while a stream is being captured into a CUDA graph.  ls_gpu_trace_report waits for
+ * the traced stages and writes one "stage count total_ms" line per stage into buffer
+ * (NUL-terminated, truncated to size); it returns the full length; reset != 0 clears the totals. */
+int ls_gpu_set_tracing(int on);
+int ls_gpu_trace_report(char *buffer, size_t size, int reset);
 /* The kernel a matvec of `op` runs: *form = 2 for the packed projected kernel (its tables fit in
  * shared memory; *slots_per_lane = group elements per lane, 32 lanes per warp), 1 for the
  * fallback projected kernel (*slots_per_lane likewise), 0 for the thread-per-row kernel (no
@@ -432,17 +450,19 @@ int ls_gpu_enumerate_noalloc(ls_hs_basis const *basis, uint64_t *d_out, int64_t 
  * 0 = each kernel's own maximum: 1024 for one right-hand side (768 for groups of more than 288
  * elements), 640 for FP64 blocks, 320 for the FP32-pair and batched kernels, lowered until the
  * shared-memory tables fit) and grid waves (the
- * grid is SMs x resident CTAs per SM x waves, one warp per row at a time; 0 = 1).  The fallback
+ * grid is SMs x resident CTAs per SM x waves, one warp per row at a time; 0 = 4).  The fallback
  * kernel for groups whose packed tables do not fit (or 64-bit states) always runs 256-thread
  * CTAs. */
 int ls_gpu_set_matvec_config(int threads_per_block, int waves);
 /* Arithmetic of complex blocks of 8 or 16 right-hand sides in the plain and the batched
- * multi-sector kernels: 0 = FP64; 1 (default) = FP32 pairs for groups of at most 64 elements,
+ * multi-sector kernels: 0 (default) = FP64; 1 = FP32 pairs for groups of at most 64 elements,
  * FP64 otherwise; 2 = FP32 pairs for every group.  In the pair form x_j * n_j is stored once per
  * call as two floats per component (16 bytes per complex element, like complex128), the
  * coefficient of each element is formed in FP64 and split, and the multiply-adds run on the
- * FP32 pipe with error-free products and two-sum accumulation (below 2^-45 relative per product;
- * H X agrees with the FP64 form to ~1e-14 relative).  With a small group and 16 columns the FP64
+ * FP32 pipe with error-free products and two-sum accumulation: each product is below 2^-45
+ * relative, so an output y_i = sum_j a_ij x_j is within about 2^-45 * sum_j |a_ij| |x_j| of the
+ * exact sum (an absolute bound: an entry that cancels to near zero keeps that error, where FP64
+ * gives ~1e-16 of the same sum); H X agrees with the FP64 form to ~1e-14 relative L2.  With a small group and 16 columns the FP64
  * form is bound by GB300's FP64 pipe (4 FP64 FMAs per element and column); with a large group
  * the integer orbit scan is the bound and FP64 is faster.  One right-hand side, real vectors and
  * blocks of 4 always run in FP64.  Returns LS_GPU_ERR_INVALID for other values. */
@@ -452,7 +472,7 @@ int ls_gpu_get_block_arithmetic(void);
 int ls_gpu_set_matvec_rhs_tile(int rhs_tile);
 int ls_gpu_get_matvec_config(int *threads_per_block, int *waves, int *rhs_tile);
 /* Autotuner: times the matvec of `op` on k complex right-hand sides over a table of
- * (threads, waves) pairs ({kernel maximum, 768, 512} x {1, 2, 4}) and, for k >= 8,
+ * (threads, waves) pairs ({kernel maximum, 768, 512} x {1, 2, 4, 8}) and, for k >= 8,
  * right-hand-side tiles, and installs the fastest; reports the launch shape (threads 0 = the
  * kernel maximum) and its time (ms). */
 int ls_gpu_autotune_matvec(ls_hs_operator const *op, int k, int *best_threads, int *best_waves,

@@ -16,7 +16,8 @@ from ._group import Symmetry, Symmetries  # noqa: F401
 from ._expr import Expr  # noqa: F401
 from . import _native  # noqa: F401
 from ._api import (Basis, Operator, SectorBatch, SpinBasis, SpinfulFermionBasis,  # noqa: F401
-                   SpinlessFermionBasis, basis_from_json, load_basis, load_library)
+                   SpinlessFermionBasis, basis_from_json, load_basis, load_library, set_tracing,
+                   stage_times)
 
 __version__ = "2.2.0+gb300"
 

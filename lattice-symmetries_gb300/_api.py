@@ -758,11 +758,11 @@ class Operator(_LinearOperator):
 
     @staticmethod
     def block_arithmetic(mode: Optional[str] = None) -> str:
-        """Arithmetic of complex blocks of 8 or 16 right-hand sides: "auto" (default: FP32-pair
-        multiply-adds from an FP64 coefficient and a prescaled pair copy of x for groups of at
-        most 64 elements, where FP64 bounds the kernel; ~1e-14 relative to the FP64 form),
-        "pairs" (pairs for every group) or "fp64".  Sets it when `mode` is given; returns the mode
-        in force."""
+        """Arithmetic of complex blocks of 8 or 16 right-hand sides: "fp64" (default), "auto"
+        (FP32-pair multiply-adds from an FP64 coefficient and a prescaled pair copy of x for
+        groups of at most 64 elements, where FP64 bounds the kernel; each output within about
+        2^-45 times the sum of its terms' magnitudes, ~1e-14 relative L2 to the FP64 form) or
+        "pairs" (pairs for every group).  Sets it when `mode` is given; returns the mode in force."""
         lib = N.lib()
         codes = Operator._ARITHMETIC
         if mode is not None:
@@ -794,6 +794,28 @@ class Operator(_LinearOperator):
 
 def load_library():
     return N.lib()
+
+
+def set_tracing(on: bool = True) -> None:
+    """Per-stage timing of the library (NVTX ranges and CUDA-event pairs around enumeration,
+    index build, orbit norms, prescale and matvec kernels, batched and coupling kernels and the
+    eigensolver's dense products); off by default.  Do not switch it on during a CUDA-graph
+    capture."""
+    N.lib().ls_gpu_set_tracing(int(bool(on)))
+
+
+def stage_times(reset: bool = True) -> dict:
+    """{stage: (launches, total milliseconds)} of the traced stages since the last reset (waits
+    for the traced work to finish)."""
+    lib = N.lib()
+    n = lib.ls_gpu_trace_report(None, 0, 0)
+    buf = ctypes.create_string_buffer(n + 1)
+    lib.ls_gpu_trace_report(ctypes.addressof(buf), n + 1, int(bool(reset)))
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, count, ms = line.split()
+        out[name] = (int(count), float(ms))
+    return out
 
 
 class SectorBatch:

@@ -183,6 +183,8 @@ _SIGNATURES = [
                                        POINTER(c_double)]),
     ("ls_gpu_count_nonzeros", c_int, [POINTER(ls_hs_operator), POINTER(c_int64)]),
     ("ls_gpu_matvec_kernel_info", c_int, [POINTER(ls_hs_operator), POINTER(c_int), POINTER(c_int)]),
+    ("ls_gpu_set_tracing", c_int, [c_int]),
+    ("ls_gpu_trace_report", c_int, [c_void_p, c_size_t, c_int]),
     ("ls_gpu_sector_plan_set_batched", c_int, [c_void_p, c_int]),
     ("ls_gpu_sector_plan_autotune", c_int, [c_void_p, c_void_p, POINTER(c_int), POINTER(c_double),
                                             POINTER(c_double)]),

@@ -1285,9 +1285,9 @@ extern "C" int ls_gpu_autotune_matvec(ls_hs_operator const* op, int k, int* best
   cudaEventCreate(&e1);
   // threads per CTA (each kernel clamps to its own maximum; 0 = that maximum) x grid waves
   const int threads_choices[] = {0, 768, 512};
-  const int wave_choices[] = {1, 2, 4};
+  const int wave_choices[] = {1, 2, 4, 8};
   double best = 1e300;
-  int bt = 0, bw = 1, rc = 0;
+  int bt = 0, bw = 4, rc = 0;
   for (int th : threads_choices) {
     for (int wv : wave_choices) {
       set_matvec_config(th, wv);
@@ -1346,6 +1346,15 @@ extern "C" int ls_gpu_check_errors(void* stream) {
   std::lock_guard<std::mutex> lock(g_mutex);
   cudaStream_t s = (cudaStream_t)stream;  // NULL: the legacy default stream (CUDA convention)
   return read_and_clear_error(s);
+}
+
+extern "C" int ls_gpu_set_tracing(int on) {
+  set_tracing(on != 0);
+  return 0;
+}
+
+extern "C" int ls_gpu_trace_report(char* buffer, size_t size, int reset) {
+  return trace_report(buffer, size, reset != 0);
 }
 
 extern "C" int ls_gpu_matvec_kernel_info(ls_hs_operator const* op, int* form, int* slots_per_lane) {

@@ -434,6 +434,7 @@ int launch_is_representative(const DeviceGroup& g0, int64_t n, const uint64_t* d
 int launch_orbit_norms(const DeviceGroup& g0, int64_t n, const uint64_t* d_reps, double* d_norms,
                        cudaStream_t s) {
   if (n <= 0) return 0;
+  StageScope stage("basis.orbit_norms", s);
   DeviceGroup g = strip(g0);
   dispatch_depth<RunNorms>(g.depth, group_is_standard(g0), g, n, d_reps, d_norms, s);
   return cuda_ok(cudaGetLastError(), "k_orbit_norms") ? 0 : LS_GPU_ERR_CUDA;
@@ -897,7 +898,10 @@ int enumerate_states(const DeviceGroup* g0, const EnumerateRequest& req, uint64_
     uint64_t* out = nullptr;
     if (!cuda_ok(cudaMalloc((void**)&out, std::max<int64_t>(n, 1) * 8), "cudaMalloc(states)"))
       return LS_GPU_ERR_CUDA;
-    k_enumerate_plain<<<grid_for((n + 15) / 16, 256), 256, 0, s>>>(r0, n, h, n_bits, out);
+    {
+      StageScope stage("basis.enumerate", s);
+      k_enumerate_plain<<<grid_for((n + 15) / 16, 256), 256, 0, s>>>(r0, n, h, n_bits, out);
+    }
     if (!cuda_ok(cudaGetLastError(), "k_enumerate_plain")) {
       cudaFree(out);
       return LS_GPU_ERR_CUDA;
@@ -920,7 +924,10 @@ int enumerate_states(const DeviceGroup* g0, const EnumerateRequest& req, uint64_
     uint64_t* out = nullptr;
     if (!cuda_ok(cudaMalloc((void**)&out, std::max<int64_t>(n, 1) * 8), "cudaMalloc(states)"))
       return LS_GPU_ERR_CUDA;
-    k_enumerate_spinful<<<grid_for(n / 16 + 1, 256), 256, 0, s>>>(rA, nA, hA, rB, nB, hB, ns, out);
+    {
+      StageScope stage("basis.enumerate", s);
+      k_enumerate_spinful<<<grid_for(n / 16 + 1, 256), 256, 0, s>>>(rA, nA, hA, rB, nB, hB, ns, out);
+    }
     if (!cuda_ok(cudaGetLastError(), "k_enumerate_spinful")) {
       cudaFree(out);
       return LS_GPU_ERR_CUDA;
@@ -968,7 +975,10 @@ int enumerate_states(const DeviceGroup* g0, const EnumerateRequest& req, uint64_
     a.capacity = capacity;
     a.counter = counter;
     cudaMemsetAsync(counter, 0, 8, s);
-    dispatch_depth<RunEnumerate>(g.depth, group_is_standard(*g0), g, a, s);
+    {
+      StageScope stage("basis.enumerate", s);
+      dispatch_depth<RunEnumerate>(g.depth, group_is_standard(*g0), g, a, s);
+    }
     if (!cuda_ok(cudaGetLastError(), "k_enumerate_projected") ||
         !cuda_ok(cudaMemcpyAsync(&total, counter, 8, cudaMemcpyDeviceToHost, s), "read count") ||
         !cuda_ok(cudaStreamSynchronize(s), "enumerate")) {
@@ -985,10 +995,15 @@ int enumerate_states(const DeviceGroup* g0, const EnumerateRequest& req, uint64_
     cleanup();
     return LS_GPU_ERR_CUDA;
   }
-  int rc = exclusive_scan<int32_t>(tile_count, a.n_tiles, tile_offset, s);
+  int rc = 0;
+  {
+    StageScope stage("basis.enumerate_compact", s);
+    rc = exclusive_scan<int32_t>(tile_count, a.n_tiles, tile_offset, s);
+    if (rc == 0)
+      k_gather_runs<<<grid_for(a.n_tiles, 256), 256, 0, s>>>(a.n_tiles, tile_count, tile_start,
+                                                            tile_offset, append, out);
+  }
   if (rc == 0) {
-    k_gather_runs<<<grid_for(a.n_tiles, 256), 256, 0, s>>>(a.n_tiles, tile_count, tile_start,
-                                                          tile_offset, append, out);
     if (!cuda_ok(cudaGetLastError(), "k_gather_runs") || !cuda_ok(cudaStreamSynchronize(s), "gather"))
       rc = LS_GPU_ERR_CUDA;
   }
@@ -1055,6 +1070,7 @@ int build_prefix_index(const uint64_t* d_reps, int64_t n, int number_bits, int p
                        uint32_t** d_offsets, int64_t* range_size, int* shift, cudaStream_t s,
                        uint64_t* max_state) {
   if (n >= ((int64_t)1 << 32)) return fail(LS_GPU_ERR_INVALID, "more than 2^32 representatives");
+  StageScope stage("basis.index", s);
   uint64_t max_rep = 0;
   if (n > 0 && !cuda_ok(cudaMemcpyAsync(&max_rep, d_reps + (n - 1), 8, cudaMemcpyDeviceToHost, s), "read max") )
     return LS_GPU_ERR_CUDA;

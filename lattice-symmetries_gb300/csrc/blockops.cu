@@ -241,6 +241,7 @@ int launch_block_gram(int64_t S, int64_t D, int k, const double* d_x, const doub
                "cudaMallocAsync(block Gram partials)"))
     return LS_GPU_ERR_CUDA;
   const dim3 grid((unsigned)chunks, (unsigned)S);
+  StageScope stage("lanczos.gram", s);
   k_block_gram<<<grid, kThreads, 0, s>>>(D, k, rows, (int)chunks, reinterpret_cast<const double2*>(d_x),
                                          reinterpret_cast<const double2*>(d_y), d_x == d_y, partial);
   bool ok = cuda_ok(cudaGetLastError(), "k_block_gram");
@@ -266,6 +267,7 @@ int launch_block_update(int64_t S, int64_t D, int k, double beta, const double* 
   const int64_t chunks = (D + rows - 1) / rows;
   if (chunks > 0x7fffffff) return fail(LS_GPU_ERR_INVALID, "block update: too many rows");
   const dim3 grid((unsigned)chunks, (unsigned)S);
+  StageScope stage("lanczos.update", s);
   k_block_update<<<grid, kThreads, 0, s>>>(D, k, rows, beta, reinterpret_cast<const double2*>(d_w),
                                            reinterpret_cast<const double2*>(d_x1),
                                            reinterpret_cast<const double2*>(d_m1),

@@ -33,8 +33,11 @@ __global__ void __launch_bounds__(256, 2)
   const int nbits = p.group.n_bits;
   const int SH = 64 - nbits;
   const uint64_t lowmask = (1ull << SH) - 1;
-  const ScanKeys keys = scan_keys(nbits);
-  uint32_t* gw = T.ga + (threadIdx.x >> 5) * 32 * rec_stride(GPL);  // this warp's g.a records
+  RowScan<GPL, INV> scan;
+  scan.rec = T.rec;
+  scan.gw = T.ga + (threadIdx.x >> 5) * 32 * rec_stride(GPL);  // this warp's g.a records
+  scan.keys = scan_keys(nbits);
+  scan.lane = lane;
   const double2* X = reinterpret_cast<const double2*>(x);
   const double2* Gv = reinterpret_cast<const double2*>(g);
   const DeviceIndex& ix = p.index;
@@ -71,9 +74,7 @@ __global__ void __launch_bounds__(256, 2)
       }
     }
 
-    __syncwarp();  // the previous row's scans have read the records
-    uint32_t gh[GPL];
-    row_images<GPL>(T.rec, gw, a, lane, gh);
+    scan.init(a);
 
     // the owning lane of each element keeps its key and term; coefficient, sign and coupling
     // are read at the flush
@@ -117,9 +118,8 @@ __global__ void __launch_bounds__(256, 2)
           }
         }
         const uint64_t key = (((info >> 16) & 0xffu) == 2u)
-                                 ? scan_two_site<GPL, INV>(T.rec, gw, gh, (int)(info & 0xffu),
-                                                           (int)((info >> 8) & 0xffu), lane, keys)
-                                 : scan_general<GPL, INV>(T.rec, gw, gh, xt, lane, keys);
+                                 ? scan.two_site((int)(info & 0xffu), (int)((info >> 8) & 0xffu))
+                                 : scan.general(xt);
         if (lane == nslot) {
           my_key = key;
           my_t = t;
@@ -187,6 +187,7 @@ int launch_coupling_products(const MatvecProblem& p, int nc, const double* d_g, 
   double2* partial = (double2*)scratch((size_t)blocks * nc * sizeof(double2), 6);
   if (partial == nullptr) return LS_GPU_ERR_CUDA;
   auto go = [&](auto kern) -> int {
+    StageScope stage("couplings.kernel", s);
     if (!ensure_smem_limit((const void*)kern, smem)) return LS_GPU_ERR_CUDA;
     kern<<<blocks, 256, smem, s>>>(p, L, off_cpl, nc, d_g, d_x, partial, d_err, binom);
     if (!cuda_ok(cudaGetLastError(), "k_coupling_products")) return LS_GPU_ERR_CUDA;

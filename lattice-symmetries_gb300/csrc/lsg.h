@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include "ls_gb300.h"
+#include "trace.h"
 
 namespace lsg {
 

@@ -54,7 +54,8 @@ int set_matvec_rhs_tile(int tile) {
 // FP64 pipe bounds the kernel (groups of at most 64 elements: a short orbit scan per element
 // against 4 FP64 FMAs per element and column); 2 = FP32 pairs for every group.  With larger
 // groups the integer orbit scan is the bound and the pair form's extra instructions cost time.
-static int g_block_pairs = 1;
+// The default is FP64 (amplitudes stay FP64 unless a caller opts into pairs).
+static int g_block_pairs = 0;
 
 int set_block_arithmetic(int mode) {
   if (mode < 0 || mode > 2) return LS_GPU_ERR_INVALID;
@@ -66,10 +67,14 @@ int get_block_arithmetic() { return g_block_pairs; }
 
 static bool use_pairs(int gpl) { return g_block_pairs == 2 || (g_block_pairs == 1 && gpl <= 2); }
 
+// Grid waves of the packed kernels when none is configured: several CTAs per SM slot over time
+// balance the uneven per-row work of the last rows.
+constexpr int kDefaultWaves = 4;
+
 // threads 0: each kernel's own maximum; waves: grid = SMs x resident CTAs per SM x waves.
 void get_matvec_config(int* threads, int* waves, int* rhs_tile) {
   if (threads) *threads = g_threads_override;
-  if (waves) *waves = g_blocks_per_sm_override > 0 ? g_blocks_per_sm_override : 1;
+  if (waves) *waves = g_blocks_per_sm_override > 0 ? g_blocks_per_sm_override : kDefaultWaves;
   if (rhs_tile) *rhs_tile = g_rhs_tile;
 }
 
@@ -102,7 +107,7 @@ __global__ void k_prescale_pairs(const double2* __restrict__ x, int64_t ldx, con
 
 int packed_launch_shape(const void* kern, int max_threads, const MatvecProblem& p, int n_sectors, int64_t rows,
                         LaunchShape* sh, PackedLayout* L) {
-  const int waves = g_blocks_per_sm_override > 0 ? g_blocks_per_sm_override : 1;
+  const int waves = g_blocks_per_sm_override > 0 ? g_blocks_per_sm_override : kDefaultWaves;
   int threads = g_threads_override > 0 ? std::min(g_threads_override, max_threads) : max_threads;
   for (; threads >= 64; threads -= 32) {
     *L = make_packed_layout(p, n_sectors, threads);
@@ -180,6 +185,7 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
       float4* d_xp = nullptr;
       if (want_fp64) {
         if (cudaMallocAsync((void**)&d_xs, (size_t)total_elems * scalar_words * sizeof(double), s) == cudaSuccess) {
+          StageScope stage("matvec.prescale", s);
           k_prescale<<<pre_blocks, 256, 0, s>>>(d_x, ldx, p.index.norms, p.n_rows, k, (int)scalar_words, d_xs);
           if (!cuda_ok(cudaGetLastError(), "k_prescale")) {
             cudaFreeAsync(d_xs, s);
@@ -192,6 +198,7 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
       }
       if (want_pairs) {
         if (cudaMallocAsync((void**)&d_xp, (size_t)total_elems * sizeof(float4), s) == cudaSuccess) {
+          StageScope stage("matvec.prescale", s);
           k_prescale_pairs<<<pre_blocks, 256, 0, s>>>(reinterpret_cast<const double2*>(d_x), ldx, p.index.norms,
                                                       p.n_rows, k, d_xp);
           if (!cuda_ok(cudaGetLastError(), "k_prescale_pairs")) {
@@ -210,6 +217,7 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
       for (const int chunk : chunks) {
         const double* xs = d_x + (size_t)done * scalar_words;
         double* ys = d_y + (size_t)done * scalar_words;
+        StageScope stage("matvec.kernel", s);
         if (d_xp != nullptr && chunk >= 8) {
           q.xs = reinterpret_cast<const double*>(d_xp + done);
           rc = launch_packed_pair(chunk, p.group.gpl, inv, q, xs, ldx, ys, ldy, d_err, binom, s);
@@ -238,6 +246,7 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
     for (int c = 0; c < k; ++c) {
       const double* xs = d_x + (size_t)c * scalar_words;
       double* ys = d_y + (size_t)c * scalar_words;
+      StageScope stage("matvec.kernel", s);
       int rc = cplx ? launch_projected_cplx_k1(gpl, inv, p, L, shf, xs, ldx, ys, ldy, d_err, binom, s)
                     : launch_projected_real(gpl, inv, p, L, shf, xs, ldx, ys, ldy, d_err, binom, s);
       if (rc != 0) return rc;
@@ -251,6 +260,7 @@ int launch_matvec(const MatvecProblem& p, Scalar sc, int k, const double* d_x, i
   blocks = std::min<int64_t>(blocks, (int64_t)num_sms() * 16);
   blocks = std::max<int64_t>(blocks, 1);
   const LaunchShape sh{(int)blocks, threads};
+  StageScope stage("matvec.kernel", s);
   return launch_plain(cplx, p.projection == 1, k, p, L, sh, d_x, ldx, d_y, ldy, d_err, binom, s);
 }
 
@@ -383,6 +393,7 @@ int sector_plan_run(const SectorPlan* plan, int* d_err, cudaStream_t s) {
       const int64_t per_sector = (plan->total_rows * plan->k + n - 1) / n;
       const int bx = (int)std::max<int64_t>(1, std::min<int64_t>((per_sector + 255) / 256,
                                                                  ((int64_t)num_sms() * 16 + n - 1) / n));
+      StageScope stage("sectors.prescale", s);
       k_prescale_pairs_sectors<<<dim3((unsigned)bx, (unsigned)n), 256, 0, s>>>(
           plan->chunks[0].d_desc, n, plan->total_rows, plan->k, plan->ldx, d_xp);
       if (!cuda_ok(cudaGetLastError(), "k_prescale_pairs_sectors")) {
@@ -396,6 +407,7 @@ int sector_plan_run(const SectorPlan* plan, int* d_err, cudaStream_t s) {
   }
   int rc = 0;
   for (const SectorPlan::Chunk& c : plan->chunks) {
+    StageScope stage("sectors.kernel", s);
     if (d_xp != nullptr && c.k >= 8)
       rc = launch_sectors_pair(c.k, plan->shared.group.gpl, inv, plan->shared, plan->n_sectors, c.d_desc,
                                plan->n_sectors, plan->total_rows, plan->ldx, plan->ldy, d_err, binom,

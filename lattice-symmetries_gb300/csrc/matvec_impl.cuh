@@ -397,12 +397,16 @@ __global__ void __launch_bounds__(256, 2)
 //
 // Site images in shared memory are kept as lane records: slot j of lane L (group element
 // e = L + 32 j) of site r is stored as its (lo, hi) 32-bit words at
-// rec[(r * 32 + L) * S + 2 j + {0, 1}], S = 2 GPL + 1.  S is odd, so the 32 lanes reading one slot
-// of their own records hit 32 distinct banks, and lanes j < GPL reading the slots of one lane's
-// record read consecutive words.  Each warp also keeps the images of its current row state
-// (g.a, with the candidate index in the low bits) in a record area of the same layout.
+// rec[(r * 32 + L) * S + 2 j + {0, 1}].  For more than 4 slots S = 2 GPL + 1 is odd, so the 32
+// lanes reading one 32-bit word of their own records hit 32 distinct banks, and lanes j < GPL
+// reading the slots of one lane's record read consecutive words.  Each warp also keeps the images
+// of its current row state (g.a, with the candidate index in the low bits) in a record area of the
+// same layout.  Up to 4 slots the scan is a plain 64-bit minimum (RowScan below) and S is even
+// with S / 2 odd, so that slots load as 8-byte words without bank conflicts in either half-warp.
 // ------------------------------------------------------------------------------------------------
-__host__ __device__ constexpr int rec_stride(int gpl) { return 2 * gpl + 1; }
+__host__ __device__ constexpr int rec_stride(int gpl) {
+  return gpl > 4 ? 2 * gpl + 1 : (gpl % 2 == 1 ? 2 * gpl : 2 * gpl + 2);
+}
 
 struct PackedLayout {
   size_t off_rec, off_ga, off_chars, off_tm, off_tl, off_tx, off_ts, off_tv, off_ti, off_dm, off_dr, off_ds, off_dv;
@@ -537,7 +541,7 @@ __device__ __forceinline__ ScanKeys scan_keys(int nbits) {
 template <int GPL>
 __device__ __forceinline__ void row_images(const uint32_t* __restrict__ rec, uint32_t* __restrict__ gw, uint64_t a,
                                            int lane, uint32_t (&gh)[GPL]) {
-  constexpr int S = 2 * GPL + 1;
+  constexpr int S = rec_stride(GPL);
   const uint32_t* recl = rec + lane * S;
   uint32_t gl[GPL];
 #pragma unroll
@@ -583,7 +587,7 @@ __device__ __forceinline__ uint64_t scan_two_site(const uint32_t* __restrict__ r
                                                   const uint32_t (&gh)[GPL], int s0, int s1, int lane,
                                                   const ScanKeys& K) {
   constexpr unsigned FULL = 0xffffffffu;
-  constexpr int S = 2 * GPL + 1;
+  constexpr int S = rec_stride(GPL);
   const uint32_t* p0 = rec + (s0 * 32 + lane) * S + 1;
   const uint32_t* p1 = rec + (s1 * 32 + lane) * S + 1;
   uint32_t mn = 0xffffffffu, mx = 0u;
@@ -619,12 +623,13 @@ __device__ __forceinline__ uint64_t scan_two_site(const uint32_t* __restrict__ r
 }
 
 // Orbit scan of beta = a ^ xt for any number of flipped sites: full 64-bit keys per slot.
+// (Groups of more than 4 slots per lane; the warp's records hold the low words of g.a.)
 template <int GPL, bool INV>
 __device__ __forceinline__ uint64_t scan_general(const uint32_t* __restrict__ rec, const uint32_t* __restrict__ gw,
                                                  const uint32_t (&gh)[GPL], uint64_t xt, int lane,
                                                  const ScanKeys& K) {
   constexpr unsigned FULL = 0xffffffffu;
-  constexpr int S = 2 * GPL + 1;
+  constexpr int S = rec_stride(GPL);
   const uint32_t* recl = rec + lane * S;
   const uint32_t* mine = gw + lane * S;
   const uint64_t fk = ((uint64_t)K.fk_hi << 32) | K.fk_lo;
@@ -650,6 +655,93 @@ __device__ __forceinline__ uint64_t scan_general(const uint32_t* __restrict__ re
   const uint32_t mlo = __reduce_min_sync(FULL, hi == mhi ? lo : 0xffffffffu);
   return ((uint64_t)mhi << 32) | mlo;
 }
+
+// The orbit scan of one warp's row: init(a) computes g.a for the lane's slots, two_site / general
+// return the packed key of a generated state.  More than 4 slots per lane: the two-pass scan
+// (high words in registers, both words in the warp's records).  Up to 4: every slot's 64-bit key
+// directly (a short scan, where the tie pass would cost more than it saves).
+template <int GPL, bool INV, bool SMALL = (GPL <= 4)>
+struct RowScan {
+  const uint32_t* rec;
+  uint32_t* gw;
+  ScanKeys keys;
+  int lane;
+  uint32_t gh[GPL];
+  __device__ __forceinline__ void init(uint64_t a) {
+    __syncwarp();  // the previous row's scans have read the records
+    row_images<GPL>(rec, gw, a, lane, gh);
+  }
+  __device__ __forceinline__ uint64_t two_site(int s0, int s1) const {
+    return scan_two_site<GPL, INV>(rec, gw, gh, s0, s1, lane, keys);
+  }
+  __device__ __forceinline__ uint64_t general(uint64_t xt) const {
+    return scan_general<GPL, INV>(rec, gw, gh, xt, lane, keys);
+  }
+};
+
+template <int GPL, bool INV>
+struct RowScan<GPL, INV, true> {
+  static constexpr int S = rec_stride(GPL);
+  const uint32_t* rec;
+  uint32_t* gw;  // unused: no tie pass
+  ScanKeys keys;
+  int lane;
+  uint64_t ga[GPL];
+  __device__ __forceinline__ const uint2* row(int site) const {
+    return reinterpret_cast<const uint2*>(rec + (site * 32 + lane) * S);
+  }
+  __device__ __forceinline__ static uint64_t word(uint2 v) { return ((uint64_t)v.y << 32) | v.x; }
+  __device__ __forceinline__ void init(uint64_t a) {
+#pragma unroll
+    for (int k = 0; k < GPL; ++k) ga[k] = 0;
+    for (uint64_t bits = a; bits != 0; bits &= bits - 1) {
+      const uint2* r = row(__ffsll((long long)bits) - 1);
+#pragma unroll
+      for (int k = 0; k < GPL; ++k) ga[k] ^= word(r[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < GPL; ++k) ga[k] |= (uint64_t)(2 * (lane + 32 * k));
+  }
+  __device__ __forceinline__ uint64_t reduce(uint64_t (&cand)[GPL]) const {
+    constexpr unsigned FULL = 0xffffffffu;
+    if (INV) {
+      const uint64_t fk = ((uint64_t)keys.fk_hi << 32) | keys.fk_lo;
+#pragma unroll
+      for (int k = 0; k < GPL; ++k) {
+        const uint32_t m = (uint32_t)((int32_t)(uint32_t)(cand[k] >> 32) >> 31);
+        cand[k] ^= fk & (((uint64_t)m << 32) | m);
+      }
+    }
+#pragma unroll
+    for (int w = 1; w < GPL; w *= 2) {
+#pragma unroll
+      for (int k = 0; k + w < GPL; k += 2 * w) cand[k] = cand[k + w] < cand[k] ? cand[k + w] : cand[k];
+    }
+    const uint32_t hi = (uint32_t)(cand[0] >> 32), lo = (uint32_t)cand[0];
+    const uint32_t mhi = __reduce_min_sync(FULL, hi);
+    const uint32_t mlo = __reduce_min_sync(FULL, hi == mhi ? lo : 0xffffffffu);
+    return ((uint64_t)mhi << 32) | mlo;
+  }
+  __device__ __forceinline__ uint64_t two_site(int s0, int s1) const {
+    const uint2* r0 = row(s0);
+    const uint2* r1 = row(s1);
+    uint64_t cand[GPL];
+#pragma unroll
+    for (int k = 0; k < GPL; ++k) cand[k] = ga[k] ^ word(r0[k]) ^ word(r1[k]);
+    return reduce(cand);
+  }
+  __device__ __forceinline__ uint64_t general(uint64_t xt) const {
+    uint64_t cand[GPL];
+#pragma unroll
+    for (int k = 0; k < GPL; ++k) cand[k] = ga[k];
+    for (uint64_t bits = xt; bits != 0; bits &= bits - 1) {
+      const uint2* r = row(__ffsll((long long)bits) - 1);
+#pragma unroll
+      for (int k = 0; k < GPL; ++k) cand[k] ^= word(r[k]);
+    }
+    return reduce(cand);
+  }
+};
 
 // One output row of the packed kernels (executed by a whole warp): y[row, 0..K) for the sector
 // described by (ix, chars, spin_inversion, x, y).
@@ -680,11 +772,14 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
   const int lane = threadIdx.x & 31;
   const int SH = 64 - nbits;
   const uint64_t lowmask = (1ull << SH) - 1;
-  const ScanKeys keys = scan_keys(nbits);
   const int rhs = lane % K;
   const int q = lane / K;
   const int nt = T.nt;
-  uint32_t* gw = T.ga + (threadIdx.x >> 5) * 32 * rec_stride(GPL);  // this warp's g.a records
+  RowScan<GPL, INV> scan;
+  scan.rec = T.rec;
+  scan.gw = T.ga + (threadIdx.x >> 5) * 32 * rec_stride(GPL);  // this warp's g.a records
+  scan.keys = scan_keys(nbits);
+  scan.lane = lane;
 
   const uint64_t a = __ldg(ix.reps + row);
   const double inv_na = __ldg(ix.inv_norms + row);
@@ -698,10 +793,8 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
     }
     return;
   }
-  // g.a for this lane's slots (high words here, both words in the warp's records)
-  __syncwarp();  // the previous row's scans have read the records
-  uint32_t gh[GPL];
-  row_images<GPL>(T.rec, gw, a, lane, gh);
+  // g.a for this lane's slots
+  scan.init(a);
 
   double dre = 0.0, dim = 0.0;
   F2 dpr{0.0f, 0.0f}, dpi{0.0f, 0.0f};  // PAIR: the diagonal element as pairs
@@ -868,8 +961,7 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
         const int t = t0 + __ffs(mask) - 1;
         mask &= mask - 1;
         const uint32_t info = T.ti[t];
-        const uint64_t key = scan_two_site<GPL, INV>(T.rec, gw, gh, (int)(info & 0xffu), (int)((info >> 8) & 0xffu),
-                                                     lane, keys);
+        const uint64_t key = scan.two_site((int)(info & 0xffu), (int)((info >> 8) & 0xffu));
         my_key = lane == nslot ? key : my_key;
         my_t = lane == nslot ? t : my_t;
         ++nslot;
@@ -895,9 +987,8 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
         }
       }
       const uint64_t key = (((info >> 16) & 0xffu) == 2u)
-                               ? scan_two_site<GPL, INV>(T.rec, gw, gh, (int)(info & 0xffu),
-                                                         (int)((info >> 8) & 0xffu), lane, keys)
-                               : scan_general<GPL, INV>(T.rec, gw, gh, xt, lane, keys);
+                               ? scan.two_site((int)(info & 0xffu), (int)((info >> 8) & 0xffu))
+                               : scan.general(xt);
       if (lane == nslot) {
         my_key = key;
         my_t = t;

@@ -2,15 +2,16 @@
 
 The path does not exchange data between GPUs: independent symmetry sectors (or independent
 copies of one workload) are assigned to ranks, and only timings and scalar results are combined
-(`torch.distributed` with NCCL on GPUs, gloo on CPU).  The reference's distributed design (hashed
-states and an all-to-all exchange per chunk, DistributedMatrixVector.chpl:179-339) is not used:
-every sector fits one GB300.
+(`torch.distributed` with NCCL on GPUs, gloo on CPU).  This is the GPU counterpart of the
+reference's split of the work among locales (chapel/src/StatesEnumeration.chpl:392-458), with
+whole sectors as the unit: every sector fits one GB300, so no state is hashed to another GPU and
+no exchange of (beta, c) pairs is needed (the reference's DistributedMatrixVector.chpl:179-339).
 """
 
 from __future__ import annotations
 
 import heapq
-from typing import List, Sequence
+from typing import Any, Dict, List, Sequence, Tuple
 
 
 def shard_by_weight(weights: Sequence[float], world: int) -> List[List[int]]:
@@ -58,3 +59,35 @@ def barrier() -> None:
     import torch.distributed as dist
     if dist.is_available() and dist.is_initialized():
         dist.barrier()
+
+
+def world_and_rank() -> Tuple[int, int]:
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        return dist.get_world_size(), dist.get_rank()
+    return 1, 0
+
+
+def my_units(weights: Sequence[float]) -> List[int]:
+    """This rank's share of the units (shard_by_weight over the process group; all units when no
+    group is initialised)."""
+    world, rank = world_and_rank()
+    return shard_by_weight(weights, world)[rank]
+
+
+def gather_results(local: Dict[int, Any]) -> Dict[int, Any]:
+    """Merges every rank's {unit: result} into one dict (all ranks receive it); a unit reported
+    twice is an error."""
+    import torch.distributed as dist
+    world, _ = world_and_rank()
+    if world == 1:
+        return dict(local)
+    parts: List[Any] = [None] * world
+    dist.all_gather_object(parts, dict(local))
+    out: Dict[int, Any] = {}
+    for part in parts:
+        for k, v in part.items():
+            if k in out:
+                raise RuntimeError("unit {} reported by two ranks".format(k))
+            out[k] = v
+    return out

@@ -190,12 +190,12 @@ def test_host_side_settings_without_a_gpu():
     dense-product shapes and NULL plans are rejected with LS_GPU_ERR_INVALID and a message."""
     lib = N.lib()
     ls_ = __import__("importlib").import_module("lattice-symmetries_gb300")
-    assert ls_.Operator.block_arithmetic() == "auto"
-    for mode in ("fp64", "pairs", "auto"):
+    assert ls_.Operator.block_arithmetic() == "fp64"
+    for mode in ("pairs", "auto", "fp64"):
         assert ls_.Operator.block_arithmetic(mode) == mode
     assert lib.ls_gpu_set_block_arithmetic(-1) == -1
     assert lib.ls_gpu_set_block_arithmetic(3) == -1
-    assert ls_.Operator.block_arithmetic() == "auto"
+    assert ls_.Operator.block_arithmetic() == "fp64"
     assert lib.ls_gpu_set_matvec_config(33, 0) == -1
     assert lib.ls_gpu_set_matvec_config(1056, 0) == -1
     assert lib.ls_gpu_set_matvec_config(0, 65) == -1
@@ -211,6 +211,11 @@ def test_host_side_settings_without_a_gpu():
     count = ctypes.c_int64(-1)
     assert lib.ls_gpu_enumerate_noalloc(basis._payload, None, 70, ctypes.byref(count), None) == -1
     assert b"NULL" in lib.ls_gpu_last_error()
+    # per-stage timing: nothing traced, an empty report, on and off again
+    assert ls_.stage_times() == {}
+    ls_.set_tracing(True)
+    assert ls_.stage_times() == {}
+    ls_.set_tracing(False)
     N.take_errors()
 
 

@@ -1,5 +1,5 @@
-"""Complex blocks of 8 and 16 right-hand sides in FP32-pair arithmetic (the default block
-arithmetic): every column against the oracle (relative L2 <= 1e-12, the tolerance of the hot
+"""Complex blocks of 8 and 16 right-hand sides in FP32-pair arithmetic (opt-in; FP64 is the
+default block arithmetic): every column against the oracle (relative L2 <= 1e-12, the tolerance of the hot
 path) and against the FP64 block kernels (relative L2 <= 1e-13), for the plain, adjoint,
 fermionic and batched multi-sector kernels."""
 
@@ -22,9 +22,9 @@ def rel_l2(a, b):
 
 @pytest.fixture
 def arithmetic():
-    """Restores the default ("auto") after each test."""
+    """Restores the default ("fp64") after each test."""
     yield ls.Operator.block_arithmetic
-    ls.Operator.block_arithmetic("auto")
+    ls.Operator.block_arithmetic("fp64")
 
 
 def both_modes(apply, arithmetic):
@@ -129,7 +129,7 @@ def test_pair_batched_sectors_match_fp64(arithmetic):
 
 
 def test_block_arithmetic_setting(arithmetic):
-    assert arithmetic() == "auto"
+    assert arithmetic() == "fp64"
     assert arithmetic("fp64") == "fp64"
     assert arithmetic() == "fp64"
     with pytest.raises(ValueError):

@@ -195,3 +195,19 @@ def test_gram_and_update_on_blocks_larger_than_l2():
     ref = Y + X @ (M1 + M2)
     bound = Y.abs() + X.abs() @ (M1.abs() + M2.abs())
     assert float(((out - ref).abs() / bound).max()) <= TOL
+
+
+def test_gram_of_orthonormal_blocks_within_the_absolute_bound():
+    """The Gram of an orthonormal block: off-diagonal entries cancel to ~1e-16, so the pair
+    kernel's error is not small relative to them; it stays within 2^-45 per product times the sum
+    of the products' magnitudes (with a factor 8 for the tile sums), the bound it documents."""
+    import torch
+    X = rand_block(2, 60000, 16, seed=21)
+    Q = torch.stack([torch.linalg.qr(X[s])[0] for s in range(X.shape[0])]).contiguous()
+    G = gram(Q, Q)
+    G64 = torch.einsum("sdi,sdj->sij", Q.conj(), Q)
+    mag = torch.einsum("sdi,sdj->sij", Q.abs(), Q.abs())
+    err = (G - G64).abs()
+    assert bool((err <= 8 * 2.0 ** -45 * mag).all())
+    off = ~torch.eye(16, dtype=torch.bool, device="cuda")
+    assert float(G64.abs()[:, off].max()) < 1e-14

@@ -60,3 +60,44 @@ def test_two_ranks_over_gloo():
         assert total == 3.0
         assert sorted(i for p in parts for i in p) == list(range(6))
         assert parts == rep.shard_by_weight([5, 4, 3, 2, 1, 1], 2)
+
+
+def _sector_worker(rank, world, port, queue):
+    """A rank of the sector split: its share of 56 sectors (LPT on their sizes), a host stand-in
+    for the GPU step (a per-sector number that depends only on the sector), max-over-ranks time
+    and the merged results."""
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        sizes = [716000 + 37 * ((s * 7919) % 101) for s in range(56)]
+        mine = rep.my_units(sizes)
+        local = {s: -0.5 * s + 1e-3 * sizes[s] for s in mine}  # stand-in for a sector's E0
+        merged = rep.gather_results(local)
+        slowest = rep.max_over_ranks(float(sum(sizes[s] for s in mine)))
+        queue.put((rank, mine, merged, slowest))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_sector_split_over_two_ranks():
+    mp = torch.multiprocessing.get_context("spawn")
+    queue = mp.Queue()
+    port = _free_port()
+    procs = [mp.Process(target=_sector_worker, args=(r, 2, port, queue)) for r in range(2)]
+    for p in procs:
+        p.start()
+    results = sorted(queue.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    sizes = [716000 + 37 * ((s * 7919) % 101) for s in range(56)]
+    serial = {s: -0.5 * s + 1e-3 * sizes[s] for s in range(56)}
+    (_, mine0, merged0, slow0), (_, mine1, merged1, slow1) = results
+    assert sorted(mine0 + mine1) == list(range(56)) and not set(mine0) & set(mine1)
+    assert merged0 == merged1 == serial
+    assert slow0 == slow1 == max(sum(sizes[s] for s in mine0), sum(sizes[s] for s in mine1))
+    # without a process group a single process takes every unit
+    assert rep.my_units(sizes) == list(range(56))
+    assert rep.gather_results({1: 2.0}) == {1: 2.0}
