@@ -919,8 +919,6 @@ def main():
     achieved_gbs = bytes_per_launch / (ms_per_step * 1e-3) / 1e9
     peak, peak_kind = load_peaks()
 
-    # block matvec (16 right-hand sides) and adjoint, per vector
-    extra = {} if args.no_extras else block_and_adjoint(op, rng, D, elements, ms_per_step, args.steps, x, y, sptr)
 
     # end to end through the reference-facing C ABI with host buffers
     e2e = None
@@ -931,19 +929,35 @@ def main():
         op.apply_to_state_vectors(xs)
         torch.cuda.synchronize()
         ne = max(1, min(args.steps, 3))
-        t0 = time.perf_counter()
+        t_calls = []
         for _ in range(ne):
+            t0 = time.perf_counter()
             ys = op.apply_to_state_vectors(xs)
-        te = (time.perf_counter() - t0) / ne
+            t_calls.append(time.perf_counter() - t0)
+        te = sum(t_calls) / ne
         # the same through two one-vector calls, as the reference's interface allows
         t0 = time.perf_counter()
         yr = op.apply_to_state_vector(np.ascontiguousarray(x_host.real))
         yi = op.apply_to_state_vector(np.ascontiguousarray(x_host.imag))
         t_two = time.perf_counter() - t0
+        # stages of one more (traced, untimed) call
+        ls.set_tracing(True)
+        t0 = time.perf_counter()
+        op.apply_to_state_vectors(xs)
+        t_traced = time.perf_counter() - t0
+        ls.set_tracing(False)
+        stages_e2e = ls.stage_times(reset=False)
+        stages_e2e_host = ls.stage_times(reset=True, host=True)
         e2e = {"value": world * elements / te, "unit": "elements/s", "h2d_bytes_per_step": 2 * 8 * D,
                "d2h_bytes_per_step": 2 * 8 * D,
                "path": "ls_chpl_matrix_vector_product(num_vectors=2: Re x, Im x), host buffers",
-               "two_single_vector_calls": {"value": world * elements / t_two}}
+               "two_single_vector_calls": {"value": world * elements / t_two},
+               "stages_ms": {k: v[1] for k, v in stages_e2e.items()},
+               "stages_host_ms": {k: v[1] for k, v in stages_e2e_host.items()},
+               "traced_call_ms": t_traced * 1e3, "calls_ms": [t * 1e3 for t in t_calls]}
+
+    # block matvec (16 right-hand sides) and adjoint, per vector
+    extra = {} if args.no_extras else block_and_adjoint(op, rng, D, elements, ms_per_step, args.steps, x, y, sptr)
 
     cpu, parity = None, None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

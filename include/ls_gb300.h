@@ -323,7 +323,8 @@ int ls_gpu_count_nonzeros(ls_hs_operator const *op, int64_t *nnz);
  * sectors.prescale, sectors.kernel, couplings.kernel, lanczos.gram, lanczos.update -- each open an
  * NVTX range and record a CUDA-event pair on their stream (no added synchronisation).  Do not
  * switch it on while a stream is being captured into a CUDA graph.  ls_gpu_trace_report waits for
- * the traced stages and writes one "stage count total_ms" line per stage into buffer
+ * the traced stages and writes one "stage count total_ms host_ms" line per stage (the time between
+ * the stage's events on the GPU, and the wall time the calling thread spent in it) into buffer
  * (NUL-terminated, truncated to size); it returns the full length; reset != 0 clears the totals. */
 int ls_gpu_set_tracing(int on);
 int ls_gpu_trace_report(char *buffer, size_t size, int reset);

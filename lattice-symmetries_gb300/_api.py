@@ -804,17 +804,18 @@ def set_tracing(on: bool = True) -> None:
     N.lib().ls_gpu_set_tracing(int(bool(on)))
 
 
-def stage_times(reset: bool = True) -> dict:
+def stage_times(reset: bool = True, host: bool = False) -> dict:
     """{stage: (launches, total milliseconds)} of the traced stages since the last reset (waits
-    for the traced work to finish)."""
+    for the traced work to finish): GPU time between the stage's events, or with host=True the
+    wall time the calling thread spent inside the stage."""
     lib = N.lib()
     n = lib.ls_gpu_trace_report(None, 0, 0)
     buf = ctypes.create_string_buffer(n + 1)
     lib.ls_gpu_trace_report(ctypes.addressof(buf), n + 1, int(bool(reset)))
     out = {}
     for line in buf.value.decode().splitlines():
-        name, count, ms = line.split()
-        out[name] = (int(count), float(ms))
+        name, count, ms, host_ms = line.split()
+        out[name] = (int(count), float(host_ms if host else ms))
     return out
 
 

@@ -10,8 +10,11 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
+
+#include <unistd.h>
 
 #include "lsg.h"
 
@@ -1182,6 +1185,27 @@ int read_and_clear_error(cudaStream_t s) {
 
 }  // namespace
 
+// Writes one word in every page of [p, p + bytes) from several host threads, so that the pages
+// of a freshly allocated output are mapped (faulted in and zeroed by the OS) while the GPU
+// computes, instead of during the device-to-host copy.  The range is an output: its contents are
+// overwritten afterwards.
+static void prefault_output(void* p, size_t bytes) {
+  const long page = sysconf(_SC_PAGESIZE);
+  const size_t step = page > 0 ? (size_t)page : 4096;
+  const size_t pages = (bytes + step - 1) / step;
+  if (pages < 256) return;  // small outputs: not worth the threads
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t nt = std::min<size_t>(std::min<size_t>(hw, 16), pages / 64);
+  auto work = [=](size_t t) {
+    volatile unsigned char* base = (volatile unsigned char*)p;
+    for (size_t q = t; q < pages; q += nt) base[q * step] = 0;
+  };
+  std::vector<std::thread> threads;
+  for (size_t t = 1; t < nt; ++t) threads.emplace_back(work, t);
+  work(0);
+  for (auto& th : threads) th.join();
+}
+
 // DistributedMatrixVector.chpl:1090-1105: y = H x on host arrays.  The reference accepts one real
 // vector; here num_vectors >= 1 vectors stored one after the other (x[v * D + i]) go through one
 // orbit scan (they are transposed on the device to the kernels' [D][k] layout).
@@ -1196,6 +1220,8 @@ extern "C" void ls_chpl_matrix_vector_product(ls_hs_operator* matrix, int num_ve
     ls_hs_error("the number of vectors must be positive");
     return;
   }
+  cudaStream_t s = default_stream();
+  StageScope call_stage("io.call", s);
   MatvecProblem p;
   int rc = make_problem(matrix, false, &p);
   if (rc != 0) {
@@ -1204,7 +1230,6 @@ extern "C" void ls_chpl_matrix_vector_product(ls_hs_operator* matrix, int num_ve
   }
   const int64_t n = p.n_rows;
   const int k = num_vectors;
-  cudaStream_t s = default_stream();
   const size_t bytes = (size_t)std::max<int64_t>(n, 1) * k * 8;
   double* d_x = (double*)scratch(bytes, 4);
   double* d_y = (double*)scratch(bytes, 5);
@@ -1215,13 +1240,41 @@ extern "C" void ls_chpl_matrix_vector_product(ls_hs_operator* matrix, int num_ve
     return;
   }
   if (n > 0) {
-    if (!cuda_ok(cudaMemcpyAsync(d_x, x, (size_t)n * k * 8, cudaMemcpyHostToDevice, s), "H2D x")) rc = LS_GPU_ERR_CUDA;
-    if (rc == 0 && k > 1) rc = launch_transpose(d_x, d_xt, k, n, s);
+    const size_t vbytes = (size_t)n * k * 8;
+    // x is pinned for the copy when the system allows it (a DMA at full speed; a pageable copy of
+    // a large host array can be staged far slower) and unpinned before returning
+    bool pinned_x = vbytes >= (1u << 20) &&
+                    cudaHostRegister((void*)x, vbytes, cudaHostRegisterReadOnly) == cudaSuccess;
+    if (!pinned_x) cudaGetLastError();  // not registered (already pinned, or unsupported): plain copy
+    const bool overlap = (const char*)y < (const char*)x + vbytes && (const char*)x < (const char*)y + vbytes;
+    {
+      StageScope stage("io.h2d", s);
+      if (!cuda_ok(cudaMemcpyAsync(d_x, x, vbytes, cudaMemcpyHostToDevice, s), "H2D x")) rc = LS_GPU_ERR_CUDA;
+    }
+    if (rc == 0 && k > 1) {
+      StageScope stage("io.transpose", s);
+      rc = launch_transpose(d_x, d_xt, k, n, s);
+    }
     if (rc == 0) rc = launch_matvec(p, Scalar::Real, k, d_xt, k, d_yt, k, device_error_word(), s);
-    if (rc == 0 && k > 1) rc = launch_transpose(d_yt, d_y, n, k, s);
-    if (rc == 0 && !cuda_ok(cudaMemcpyAsync(y, d_y, (size_t)n * k * 8, cudaMemcpyDeviceToHost, s), "D2H y"))
-      rc = LS_GPU_ERR_CUDA;
+    if (rc == 0 && k > 1) {
+      StageScope stage("io.transpose", s);
+      rc = launch_transpose(d_yt, d_y, n, k, s);
+    }
+    // the host maps y's pages while the GPU computes (the copy below waits for the kernels); not
+    // when y overlaps x, whose copy may still be in flight
+    if (rc == 0 && !overlap) {
+      StageScope stage("io.prefault", s);
+      prefault_output(y, vbytes);
+    }
+    if (rc == 0) {
+      StageScope stage("io.d2h", s);
+      if (!cuda_ok(cudaMemcpyAsync(y, d_y, vbytes, cudaMemcpyDeviceToHost, s), "D2H y")) rc = LS_GPU_ERR_CUDA;
+    }
     if (rc == 0) rc = read_and_clear_error(s);
+    if (pinned_x) {
+      if (rc != 0) cudaStreamSynchronize(s);  // the copy of x has finished before x is unpinned
+      cudaHostUnregister((void*)x);
+    }
   }
   if (rc != 0) report("ls_chpl_matrix_vector_product");
 }

@@ -16,7 +16,7 @@ int launch_packed_fermi(bool cplx, int k, int gpl, const MatvecProblem& p, const
     };
     if (!cplx) {
       if (k != 1) return LS_GPU_ERR_INVALID;
-      return go(k_matvec_packed<G, false, false, 1, true>, PackedBounds<G, 1, false>::threads);
+      return go(k_matvec_packed<G, false, false, 1, true>, PackedBounds<G, 1, false, false>::threads);
     }
     switch (k) {
       case 1: return go(k_matvec_packed<G, false, true, 1, true>, PackedBounds<G, 1, false>::threads);

@@ -1051,19 +1051,20 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
   }
 }
 
-// Launch bounds of the packed single-sector kernels.  The one-vector kernels run CTAs of up to
-// 1024 threads (at most 64 registers per thread; 768 threads and 85 registers for groups of more
-// than 288 elements): one CTA per SM, whose 32 warps share one copy of the tables; multi-column
-// FP64 kernels up to 640 threads (102 registers); the pair kernels keep 320-thread CTAs, three
-// per SM on small groups (more warps to hide the gathers' latency).
-template <int GPL, int K, bool PAIR>
+// Launch bounds of the packed single-sector kernels.  Kernels with at most two FP64 accumulators
+// per lane (one complex or up to two real right-hand sides) run CTAs of up to 1024 threads (at
+// most 64 registers per thread; 768 threads and 85 registers for groups of more than 288
+// elements): one CTA per SM, whose 32 warps share one copy of the tables; wider FP64 blocks up to
+// 640 threads (102 registers); the pair kernels keep 320-thread CTAs, three per SM on small
+// groups (more warps to hide the gathers' latency).
+template <int GPL, int K, bool PAIR, bool CPLX = true>
 struct PackedBounds {
-  static constexpr int threads = PAIR ? 320 : (K == 1 ? (GPL <= 9 ? 1024 : 768) : 640);
+  static constexpr int threads = PAIR ? 320 : (K * (CPLX ? 2 : 1) <= 2 ? (GPL <= 9 ? 1024 : 768) : 640);
   static constexpr int min_blocks = PAIR ? ((GPL <= 2) ? 3 : 2) : 1;
 };
 
 template <int GPL, bool INV, bool CPLX, int K, bool FERMI = false, bool PAIR = false>
-__global__ void __launch_bounds__(PackedBounds<GPL, K, PAIR>::threads, PackedBounds<GPL, K, PAIR>::min_blocks)
+__global__ void __launch_bounds__(PackedBounds<GPL, K, PAIR, CPLX>::threads, PackedBounds<GPL, K, PAIR, CPLX>::min_blocks)
     k_matvec_packed(const MatvecProblem p, const PackedLayout L, const double* __restrict__ x, int64_t ldx,
                     double* __restrict__ y, int64_t ldy, int* __restrict__ err,
                     const uint64_t* __restrict__ binom) {

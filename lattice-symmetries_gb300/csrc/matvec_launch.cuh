@@ -57,7 +57,7 @@ static int launch_packed_kernel(Kernel kern, int max_threads, const char* name, 
            int64_t ldy, int* err, const uint64_t* binom, cudaStream_t s) {                        \
     auto run = [&](auto gtag) -> int {                                                            \
       constexpr int G = decltype(gtag)::value;                                                    \
-      constexpr int MT = PackedBounds<G, K, false>::threads;                                      \
+      constexpr int MT = PackedBounds<G, K, false, CPLX>::threads;                                \
       return inv ? launch_packed_kernel(k_matvec_packed<G, true, CPLX, K>, MT, #NAME, p, x, ldx,  \
                                         y, ldy, err, binom, s)                                   \
                  : launch_packed_kernel(k_matvec_packed<G, false, CPLX, K>, MT, #NAME, p, x, ldx, \

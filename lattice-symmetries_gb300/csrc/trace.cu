@@ -9,6 +9,7 @@
 // would become graph nodes that the report cannot read).
 #include <nvtx3/nvToolsExt.h>
 
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -24,11 +25,17 @@ namespace {
 struct Pending {
   const char* name;
   cudaEvent_t start, stop;
+  double host_ms;  // wall time the host spent inside the scope
 };
 struct Total {
   int64_t count = 0;
   double ms = 0.0;
+  double host_ms = 0.0;
 };
+
+double host_now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
 
 std::mutex g_trace_mutex;
 bool g_tracing = false;
@@ -58,6 +65,7 @@ void resolve_locked() {
       Total& t = g_totals[p.name];
       t.count += 1;
       t.ms += ms;
+      t.host_ms += p.host_ms;
     } else {
       cudaGetLastError();
     }
@@ -83,14 +91,16 @@ StageScope::StageScope(const char* name, cudaStream_t s) : name_(name), stream_(
   active_ = true;
   nvtxRangePushA(name);
   cudaEventRecord(start_, stream_);
+  host_start_ms_ = host_now_ms();
 }
 
 StageScope::~StageScope() {
   if (!active_) return;
+  const double host_ms = host_now_ms() - host_start_ms_;
   std::lock_guard<std::mutex> lock(g_trace_mutex);
   cudaEventRecord(stop_, stream_);
   nvtxRangePop();
-  g_pending.push_back(Pending{name_, start_, stop_});
+  g_pending.push_back(Pending{name_, start_, stop_, host_ms});
 }
 
 void set_tracing(bool on) {
@@ -104,7 +114,8 @@ int trace_report(char* buffer, size_t size, bool reset) {
   std::string out;
   char line[256];
   for (const auto& kv : g_totals) {
-    snprintf(line, sizeof(line), "%s %lld %.6f\n", kv.first.c_str(), (long long)kv.second.count, kv.second.ms);
+    snprintf(line, sizeof(line), "%s %lld %.6f %.6f\n", kv.first.c_str(), (long long)kv.second.count, kv.second.ms,
+             kv.second.host_ms);
     out += line;
   }
   if (reset) g_totals.clear();

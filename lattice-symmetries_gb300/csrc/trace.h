@@ -9,8 +9,10 @@ namespace lsg {
 
 bool tracing();
 void set_tracing(bool on);
-// Writes "stage count total_ms" lines (sorted by stage) into buffer (NUL-terminated, truncated to
-// size) after waiting for every traced stage; returns the full length.  reset clears the totals.
+// Writes "stage count total_ms host_ms" lines (sorted by stage; total_ms between the stage's CUDA
+// events, host_ms the wall time the host spent inside the scope) into buffer (NUL-terminated,
+// truncated to size) after waiting for every traced stage; returns the full length.  reset clears
+// the totals.
 int trace_report(char* buffer, size_t size, bool reset);
 
 // A traced stage: an NVTX range and a CUDA-event pair on `s` around the scope's work, when
@@ -26,6 +28,7 @@ class StageScope {
   const char* name_;
   cudaStream_t stream_;
   cudaEvent_t start_ = nullptr, stop_ = nullptr;
+  double host_start_ms_ = 0.0;
   bool active_ = false;
 };
 
