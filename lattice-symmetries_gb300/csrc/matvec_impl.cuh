@@ -796,36 +796,6 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
   // g.a for this lane's slots
   scan.init(a);
 
-  double dre = 0.0, dim = 0.0;
-  F2 dpr{0.0f, 0.0f}, dpi{0.0f, 0.0f};  // PAIR: the diagonal element as pairs
-  if constexpr (PAIR) {
-    for (int t = lane; t < T.nd; t += 32) {
-      if ((a & T.dm[t]) == T.dr[t]) {
-        const double2 v = T.dv[t];
-        const bool neg = __popcll(a & T.ds[t]) & 1;
-        const F2 vr = split_double(v.x), vi = split_double(v.y);
-        dpr = pair_add(dpr, neg ? pair_neg(vr) : vr);
-        dpi = pair_add(dpi, neg ? pair_neg(vi) : vi);
-      }
-    }
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-      dpr = pair_add(dpr, pair_shfl_xor(dpr, d));
-      dpi = pair_add(dpi, pair_shfl_xor(dpi, d));
-    }
-  } else {
-    for (int t = lane; t < T.nd; t += 32) {
-      if ((a & T.dm[t]) == T.dr[t]) {
-        const double2 v = T.dv[t];
-        const bool neg = __popcll(a & T.ds[t]) & 1;
-        dre += neg ? -v.x : v.x;
-        if constexpr (CPLX) dim += neg ? -v.y : v.y;
-      }
-    }
-    dre = warp_sum(dre);
-    if constexpr (CPLX) dim = warp_sum(dim);
-  }
-
   Acc acc;
   F2 pre{0.0f, 0.0f}, pim{0.0f, 0.0f};  // PAIR: this lane's pair sums
   unsigned found = 0;
@@ -1000,6 +970,38 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
     }
   }
   if (nslot > 0) flush();
+
+  // the diagonal element, after the off-diagonal scan (its sums are not live across the scan)
+  double dre = 0.0, dim = 0.0;
+  F2 dpr{0.0f, 0.0f}, dpi{0.0f, 0.0f};  // PAIR: the diagonal element as pairs
+  if constexpr (PAIR) {
+    for (int t = lane; t < T.nd; t += 32) {
+      if ((a & T.dm[t]) == T.dr[t]) {
+        const double2 v = T.dv[t];
+        const bool neg = __popcll(a & T.ds[t]) & 1;
+        const F2 vr = split_double(v.x), vi = split_double(v.y);
+        dpr = pair_add(dpr, neg ? pair_neg(vr) : vr);
+        dpi = pair_add(dpi, neg ? pair_neg(vi) : vi);
+      }
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      dpr = pair_add(dpr, pair_shfl_xor(dpr, d));
+      dpi = pair_add(dpi, pair_shfl_xor(dpi, d));
+    }
+  } else {
+    for (int t = lane; t < T.nd; t += 32) {
+      if ((a & T.dm[t]) == T.dr[t]) {
+        const double2 v = T.dv[t];
+        const bool neg = __popcll(a & T.ds[t]) & 1;
+        dre += neg ? -v.x : v.x;
+        if constexpr (CPLX) dim += neg ? -v.y : v.y;
+      }
+    }
+    dre = warp_sum(dre);
+    if constexpr (CPLX) dim = warp_sum(dim);
+  }
+
   if constexpr (PAIR) {
     // FP32-pair epilogue: lanes with the same column combine, then
     // y = acc / n_a + diag x_a, all in pairs; two FP64 adds per output
