@@ -582,18 +582,35 @@ __device__ __forceinline__ void row_images(const uint32_t* __restrict__ rec, uin
 // min and one max per slot.  Pass 2: only lanes whose pass-1 minimum ties the warp's take part;
 // for each, lanes j < GPL rebuild the exact key of its slot j and keep the lowest low word among
 // the keys whose high word is the minimum.
+// 32-bit shared-memory loads at explicit shared-window addresses (the record tables are written
+// before the block's first barrier and read-only afterwards; the per-warp g.a records use the
+// volatile form, ordered with the warp's record stores and __syncwarp).
+__device__ __forceinline__ uint32_t lds_u32(uint32_t addr) {
+  uint32_t v;
+  asm("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
+  return v;
+}
+__device__ __forceinline__ uint32_t lds_u32_volatile(uint32_t addr) {
+  uint32_t v;
+  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+  return v;
+}
+
 template <int GPL, bool INV>
 __device__ __forceinline__ uint64_t scan_two_site(const uint32_t* __restrict__ rec, const uint32_t* __restrict__ gw,
                                                   const uint32_t (&gh)[GPL], int s0, int s1, int lane,
                                                   const ScanKeys& K) {
   constexpr unsigned FULL = 0xffffffffu;
   constexpr int S = rec_stride(GPL);
-  const uint32_t* p0 = rec + (s0 * 32 + lane) * S + 1;
-  const uint32_t* p1 = rec + (s1 * 32 + lane) * S + 1;
+  constexpr uint32_t ROW = 32u * S * 4u;  // bytes per site
+  const uint32_t rec_s = (uint32_t)__cvta_generic_to_shared(rec);
+  const uint32_t gw_s = (uint32_t)__cvta_generic_to_shared(gw);
+  const uint32_t r0 = rec_s + (uint32_t)s0 * ROW, r1 = rec_s + (uint32_t)s1 * ROW;
+  const uint32_t p0 = r0 + (uint32_t)(lane * S * 4 + 4), p1 = r1 + (uint32_t)(lane * S * 4 + 4);
   uint32_t mn = 0xffffffffu, mx = 0u;
 #pragma unroll
   for (int k = 0; k < GPL; ++k) {
-    const uint32_t h = gh[k] ^ p0[2 * k] ^ p1[2 * k];
+    const uint32_t h = gh[k] ^ lds_u32(p0 + 8 * k) ^ lds_u32(p1 + 8 * k);
     mn = min(mn, h);
     if (INV) mx = max(mx, h);
   }
@@ -601,16 +618,14 @@ __device__ __forceinline__ uint64_t scan_two_site(const uint32_t* __restrict__ r
   const uint32_t mhi = __reduce_min_sync(FULL, lm);
   unsigned M = __ballot_sync(FULL, lm == mhi);
   // lanes beyond the slots repeat the last slot (same candidate): no divergent branch
-  const int jj = lane < GPL ? lane : GPL - 1;
-  const uint32_t* q0 = rec + s0 * 32 * S + 2 * jj;
-  const uint32_t* q1 = rec + s1 * 32 * S + 2 * jj;
-  const uint32_t* qg = gw + 2 * jj;
+  const uint32_t jj8 = (uint32_t)((lane < GPL ? lane : GPL - 1) * 8);
+  const uint32_t q0 = r0 + jj8, q1 = r1 + jj8, qg = gw_s + jj8;
   uint32_t blo = 0xffffffffu;
   do {
-    const int o = (__ffs(M) - 1) * S;
+    const uint32_t o = (uint32_t)(__ffs(M) - 1) * (uint32_t)(S * 4);
     M &= M - 1;
-    uint32_t lo = qg[o] ^ q0[o] ^ q1[o];
-    uint32_t hi = qg[o + 1] ^ q0[o + 1] ^ q1[o + 1];
+    uint32_t lo = lds_u32_volatile(qg + o) ^ lds_u32(q0 + o) ^ lds_u32(q1 + o);
+    uint32_t hi = lds_u32_volatile(qg + o + 4) ^ lds_u32(q0 + o + 4) ^ lds_u32(q1 + o + 4);
     if (INV) {  // flip when the top state bit is set: all-ones mask from the sign bit
       const uint32_t f = (uint32_t)((int32_t)hi >> 31);
       lo ^= K.fk_lo & f;
