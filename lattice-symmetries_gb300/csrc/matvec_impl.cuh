@@ -535,53 +535,6 @@ __device__ __forceinline__ ScanKeys scan_keys(int nbits) {
   return ScanKeys{(uint32_t)(flipkey >> 32), (uint32_t)flipkey, (uint32_t)(flipkey >> 32)};
 }
 
-// g.a for this lane's slots (XOR of the images of a's set bits, two sites at a time), with the
-// candidate index 2 * (lane + 32 k) in the low bits: the high words are returned in gh, both
-// words go to this lane's record of the warp's area gw (read by the tie pass of scan_two_site).
-template <int GPL>
-__device__ __forceinline__ void row_images(const uint32_t* __restrict__ rec, uint32_t* __restrict__ gw, uint64_t a,
-                                           int lane, uint32_t (&gh)[GPL]) {
-  constexpr int S = rec_stride(GPL);
-  const uint32_t* recl = rec + lane * S;
-  uint32_t gl[GPL];
-#pragma unroll
-  for (int k = 0; k < GPL; ++k) gl[k] = gh[k] = 0u;
-  uint64_t bits = a;
-  while (bits != 0) {
-    const uint32_t* r0 = recl + (__ffsll((long long)bits) - 1) * 32 * S;
-    bits &= bits - 1;
-    if (bits == 0) {
-#pragma unroll
-      for (int k = 0; k < GPL; ++k) {
-        gl[k] ^= r0[2 * k];
-        gh[k] ^= r0[2 * k + 1];
-      }
-      break;
-    }
-    const uint32_t* r1 = recl + (__ffsll((long long)bits) - 1) * 32 * S;
-    bits &= bits - 1;
-#pragma unroll
-    for (int k = 0; k < GPL; ++k) {
-      gl[k] ^= r0[2 * k] ^ r1[2 * k];
-      gh[k] ^= r0[2 * k + 1] ^ r1[2 * k + 1];
-    }
-  }
-  uint32_t* mine = gw + lane * S;
-#pragma unroll
-  for (int k = 0; k < GPL; ++k) {
-    mine[2 * k] = gl[k] | (uint32_t)(2 * (lane + 32 * k));
-    mine[2 * k + 1] = gh[k];
-  }
-  __syncwarp();
-}
-
-// Orbit scan of beta = a ^ (sites s0, s1): the smallest 64-bit key over all slots (and their spin
-// flips), i.e. (representative << SH) | (2 * element + flipped), the same key as a full 64-bit
-// minimum.  Pass 1: per slot the high word h = g.a ^ image(s0) ^ image(s1); with spin inversion
-// the candidate is min(h, flip(h)) and min over slots of that is min(min h, flip(max h)), so one
-// min and one max per slot.  Pass 2: only lanes whose pass-1 minimum ties the warp's take part;
-// for each, lanes j < GPL rebuild the exact key of its slot j and keep the lowest low word among
-// the keys whose high word is the minimum.
 // 32-bit shared-memory loads at explicit shared-window addresses (the record tables are written
 // before the block's first barrier and read-only afterwards; the per-warp g.a records use the
 // volatile form, ordered with the warp's record stores and __syncwarp).
@@ -595,7 +548,63 @@ __device__ __forceinline__ uint32_t lds_u32_volatile(uint32_t addr) {
   asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
   return v;
 }
+__device__ __forceinline__ uint64_t lds_u64(uint32_t addr) {
+  uint64_t v;
+  asm("ld.shared.u64 %0, [%1];" : "=l"(v) : "r"(addr));
+  return v;
+}
+__device__ __forceinline__ void sts_u32_volatile(uint32_t addr, uint32_t v) {
+  asm volatile("st.shared.u32 [%0], %1;" : : "r"(addr), "r"(v) : "memory");
+}
 
+// g.a for this lane's slots (XOR of the images of a's set bits, two sites at a time), with the
+// candidate index 2 * (lane + 32 k) in the low bits: the high words are returned in gh, both
+// words go to this lane's record of the warp's area gw (read by the tie pass of scan_two_site).
+template <int GPL>
+__device__ __forceinline__ void row_images(const uint32_t* __restrict__ rec, uint32_t* __restrict__ gw, uint64_t a,
+                                           int lane, uint32_t (&gh)[GPL]) {
+  constexpr int S = rec_stride(GPL);
+  constexpr uint32_t ROW = 32u * S * 4u;  // bytes per site
+  const uint32_t recl = (uint32_t)__cvta_generic_to_shared(rec) + (uint32_t)(lane * S * 4);
+  uint32_t gl[GPL];
+#pragma unroll
+  for (int k = 0; k < GPL; ++k) gl[k] = gh[k] = 0u;
+  uint64_t bits = a;
+  while (bits != 0) {
+    const uint32_t r0 = recl + (uint32_t)(__ffsll((long long)bits) - 1) * ROW;
+    bits &= bits - 1;
+    if (bits == 0) {
+#pragma unroll
+      for (int k = 0; k < GPL; ++k) {
+        gl[k] ^= lds_u32(r0 + 8 * k);
+        gh[k] ^= lds_u32(r0 + 8 * k + 4);
+      }
+      break;
+    }
+    const uint32_t r1 = recl + (uint32_t)(__ffsll((long long)bits) - 1) * ROW;
+    bits &= bits - 1;
+#pragma unroll
+    for (int k = 0; k < GPL; ++k) {
+      gl[k] ^= lds_u32(r0 + 8 * k) ^ lds_u32(r1 + 8 * k);
+      gh[k] ^= lds_u32(r0 + 8 * k + 4) ^ lds_u32(r1 + 8 * k + 4);
+    }
+  }
+  const uint32_t mine = (uint32_t)__cvta_generic_to_shared(gw) + (uint32_t)(lane * S * 4);
+#pragma unroll
+  for (int k = 0; k < GPL; ++k) {
+    sts_u32_volatile(mine + 8 * k, gl[k] | (uint32_t)(2 * (lane + 32 * k)));
+    sts_u32_volatile(mine + 8 * k + 4, gh[k]);
+  }
+  __syncwarp();
+}
+
+// Orbit scan of beta = a ^ (sites s0, s1): the smallest 64-bit key over all slots (and their spin
+// flips), i.e. (representative << SH) | (2 * element + flipped), the same key as a full 64-bit
+// minimum.  Pass 1: per slot the high word h = g.a ^ image(s0) ^ image(s1); with spin inversion
+// the candidate is min(h, flip(h)) and min over slots of that is min(min h, flip(max h)), so one
+// min and one max per slot.  Pass 2: only lanes whose pass-1 minimum ties the warp's take part;
+// for each, lanes j < GPL rebuild the exact key of its slot j and keep the lowest low word among
+// the keys whose high word is the minimum.
 template <int GPL, bool INV>
 __device__ __forceinline__ uint64_t scan_two_site(const uint32_t* __restrict__ rec, const uint32_t* __restrict__ gw,
                                                   const uint32_t (&gh)[GPL], int s0, int s1, int lane,
@@ -932,20 +941,26 @@ __device__ __forceinline__ void packed_row(const PackedTables& T, const int nbit
   if (T.all2) {
     // Every term flips two sites and keeps the conserved numbers (warp-uniform): batches of up
     // to 32 elements are scanned in a tight loop, each batch then flushed.
+    const uint32_t tm_s = (uint32_t)__cvta_generic_to_shared(T.tm);
+    const uint32_t tl_s = (uint32_t)__cvta_generic_to_shared(T.tl);
+    const uint32_t ti_s = (uint32_t)__cvta_generic_to_shared(T.ti);
     int t0 = 0;
-    unsigned mask = __ballot_sync(FULL, lane < nt && (a & T.tm[lane]) == T.tl[lane]);
+    // lanes past the last term read term 0 (inside the table) and do not match
+    unsigned mask = __ballot_sync(FULL, lane < nt && (a & lds_u64(tm_s + (lane < nt ? 8u * lane : 0u))) ==
+                                                         lds_u64(tl_s + (lane < nt ? 8u * lane : 0u)));
     for (;;) {
       nslot = 0;
       while (nslot < 32) {
         while (mask == 0 && t0 + 32 < nt) {
           t0 += 32;
-          const int tt = t0 + lane;
-          mask = __ballot_sync(FULL, tt < nt && (a & T.tm[tt]) == T.tl[tt]);
+          const bool in = t0 + lane < nt;
+          const uint32_t o = in ? 8u * (uint32_t)(t0 + lane) : 0u;  // lanes past the terms read term 0
+          mask = __ballot_sync(FULL, in && (a & lds_u64(tm_s + o)) == lds_u64(tl_s + o));
         }
         if (mask == 0) break;
         const int t = t0 + __ffs(mask) - 1;
         mask &= mask - 1;
-        const uint32_t info = T.ti[t];
+        const uint32_t info = lds_u32(ti_s + 4u * (uint32_t)t);
         const uint64_t key = scan.two_site((int)(info & 0xffu), (int)((info >> 8) & 0xffu));
         my_key = lane == nslot ? key : my_key;
         my_t = lane == nslot ? t : my_t;
