@@ -508,7 +508,7 @@ extern "C" ls_hs_state_index_binary_search_data* ls_hs_create_state_index_binary
   int64_t range = 0;
   uint64_t max_state = 0;
   if (build_prefix_index(ix->d_reps, ix->n_states, number_bits, ix->prefix_bits, &ix->d_offsets,
-                         &range, &shift, s, &max_state) != 0 ||
+                         &range, &shift, s, &max_state, &ix->d_suffix) != 0 ||
       !cuda_ok(cudaStreamSynchronize(s), "build index")) {
     report("ls_hs_create_state_index_binary_search_kernel_data");
     cudaFree(ix->d_reps);
@@ -518,6 +518,7 @@ extern "C" ls_hs_state_index_binary_search_data* ls_hs_create_state_index_binary
   ix->dev.n_states = ix->n_states;
   ix->dev.reps = ix->d_reps;
   ix->dev.offsets = ix->d_offsets;
+  ix->dev.suffix16 = ix->d_suffix;
   ix->dev.shift = shift;
   ix->dev.range_size = range;
   ix->dev.prefix_bits = ix->prefix_bits;
@@ -530,6 +531,7 @@ extern "C" void ls_hs_destroy_state_index_binary_search_kernel_data(
   if (cache == nullptr || cache->magic != kIndexMagic) return;
   cudaFree(cache->d_reps);
   cudaFree(cache->d_offsets);
+  cudaFree(cache->d_suffix);
   cudaFree(cache->d_norms);
   cache->magic = 0;
   delete cache;

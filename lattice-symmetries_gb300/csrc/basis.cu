@@ -1053,11 +1053,11 @@ __global__ void k_bucket_max(const uint32_t* __restrict__ offsets, int64_t n_buc
   if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
-__global__ void k_bucket_clamp(uint32_t* __restrict__ offsets, int64_t n_buckets, int64_t limit) {
-  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < n_buckets;
-       b += (int64_t)gridDim.x * blockDim.x) {
-    if ((int64_t)offsets[b] > limit) offsets[b] = (uint32_t)limit;
-  }
+// suffix[i] = the low `shift` bits of reps[i] (shift <= 16).
+__global__ void k_key_suffixes(const uint64_t* __restrict__ reps, int64_t n, int shift, uint16_t* __restrict__ suffix) {
+  const uint64_t mask = (1ull << shift) - 1;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    suffix[i] = (uint16_t)(reps[i] & mask);
 }
 
 // The reference buckets on the top prefix_bits of number_bits (indexing.c:94-117).  Sorted
@@ -1068,7 +1068,7 @@ __global__ void k_bucket_clamp(uint32_t* __restrict__ offsets, int64_t n_buckets
 // indices.
 int build_prefix_index(const uint64_t* d_reps, int64_t n, int number_bits, int prefix_bits,
                        uint32_t** d_offsets, int64_t* range_size, int* shift, cudaStream_t s,
-                       uint64_t* max_state) {
+                       uint64_t* max_state, uint16_t** d_suffix) {
   if (n >= ((int64_t)1 << 32)) return fail(LS_GPU_ERR_INVALID, "more than 2^32 representatives");
   StageScope stage("basis.index", s);
   uint64_t max_rep = 0;
@@ -1102,13 +1102,22 @@ int build_prefix_index(const uint64_t* d_reps, int64_t n, int number_bits, int p
     cudaFree(mx);
     return LS_GPU_ERR_CUDA;
   }
-  k_bucket_clamp<<<grid_for(nb, 256), 256, 0, s>>>(off, nb, n - (int64_t)r);
   cudaFree(mx);
-  if (!cuda_ok(cudaGetLastError(), "k_bucket_clamp")) {
-    cudaFree(off);
-    return LS_GPU_ERR_CUDA;
+  uint16_t* suf = nullptr;
+  if (*shift <= 16 && n > 0) {
+    if (!cuda_ok(cudaMalloc((void**)&suf, (size_t)n * 2), "alloc suffixes")) {
+      cudaFree(off);
+      return LS_GPU_ERR_CUDA;
+    }
+    k_key_suffixes<<<grid_for(n, 256), 256, 0, s>>>(d_reps, n, *shift, suf);
+    if (!cuda_ok(cudaGetLastError(), "k_key_suffixes")) {
+      cudaFree(off);
+      cudaFree(suf);
+      return LS_GPU_ERR_CUDA;
+    }
   }
   *d_offsets = off;
+  *d_suffix = suf;
   *range_size = (int64_t)r;
   return 0;
 }
@@ -1118,7 +1127,23 @@ __device__ __forceinline__ int64_t index_lookup(const DeviceIndex& ix, uint64_t 
   if (ix.combinadic) return d_rank(needle) - ix.rank_base;
   int64_t len = ix.range_size;
   if (len <= 0 || needle > ix.max_state) return -1;
-  int64_t base = __ldg(ix.offsets + (needle >> ix.shift));
+  const uint64_t b = needle >> ix.shift;
+  if (ix.suffix16 != nullptr) {
+    // binary search of the needle's bucket [start, end) in its 2-byte suffixes
+    const uint16_t target = (uint16_t)(needle & ((1ull << ix.shift) - 1));
+    int64_t base = __ldg(ix.offsets + b);
+    const int64_t end = __ldg(ix.offsets + b + 1);
+    int64_t n = end - base;
+    if (n <= 0) return -1;
+    while (n > 1) {
+      const int64_t half = n >> 1;
+      base = (__ldg(ix.suffix16 + base + half) <= target) ? base + half : base;
+      n -= half;
+    }
+    return __ldg(ix.suffix16 + base) == target ? base : -1;
+  }
+  // a window of the largest bucket's length starting at the bucket, moved back to end at n
+  int64_t base = min((int64_t)__ldg(ix.offsets + b), ix.n_states - len);
   while (len > 1) {
     const int64_t half = len >> 1;
     base = (__ldg(ix.reps + base + half) < needle) ? base + half : base;

@@ -75,9 +75,13 @@ struct DeviceIndex {
   const uint64_t* reps = nullptr;
   const double* norms = nullptr;      // state_info norms of the representatives
   const double* inv_norms = nullptr;  // 1 / norm (0 for a zero norm): no division per row
-  const uint32_t* offsets = nullptr;  // [2^prefix_bits + 1] window starts (clamped), or null
+  const uint32_t* offsets = nullptr;  // [2^prefix_bits + 1] bucket starts, or null
+  // Low `shift` bits of every representative (shift <= 16), or null: a lookup then scans the
+  // needle's bucket [offsets[b], offsets[b + 1]) in these 2-byte suffixes instead of searching
+  // a window of 8-byte representatives.
+  const uint16_t* suffix16 = nullptr;
   int shift = 0;                      // bucket = state >> shift
-  int64_t range_size = 0;             // window length
+  int64_t range_size = 0;             // largest bucket (window length of the search without suffixes)
   int prefix_bits = 0;
   uint64_t max_state = ~0ull;         // largest representative (larger needles are absent)
   int identity = 0;                   // index(state) = state
@@ -141,6 +145,7 @@ struct IndexData {
   DeviceIndex dev;
   uint64_t* d_reps = nullptr;
   uint32_t* d_offsets = nullptr;
+  uint16_t* d_suffix = nullptr;       // 2-byte key suffixes (shift <= 16)
   double* d_norms = nullptr;          // filled lazily when a projected matvec needs them
   const OrbitData* norms_for = nullptr;
 };
@@ -190,9 +195,12 @@ int enumerate_states_noalloc(const OrbitData* od, const EnumerateRequest& req, u
 // out[i] = sum_{k<i} in[k] for i <= n (out has n + 1 entries); stream-ordered.
 int exclusive_scan_counts(const int32_t* d_in, int64_t n, int64_t* d_out, cudaStream_t s);
 
+// Bucket starts over the top bits actually used (unclamped: bucket b is [off[b], off[b + 1])),
+// the largest bucket, and, where the bucket shift is at most 16 bits, the 2-byte key suffixes
+// (*d_suffix, else null).
 int build_prefix_index(const uint64_t* d_reps, int64_t n, int number_bits, int prefix_bits,
                        uint32_t** d_offsets, int64_t* range_size, int* shift, cudaStream_t s,
-                       uint64_t* max_state);
+                       uint64_t* max_state, uint16_t** d_suffix);
 int launch_state_index(const DeviceIndex& ix, int64_t n, const uint64_t* d_x, int64_t* d_out,
                        cudaStream_t s);
 

@@ -51,7 +51,23 @@ __device__ __forceinline__ int64_t mv_index_lookup(const DeviceIndex& ix, uint64
   }
   int64_t len = ix.range_size;
   if (len <= 0 || needle > ix.max_state) return -1;
-  int64_t base = __ldg(ix.offsets + (needle >> ix.shift));
+  const uint64_t b = needle >> ix.shift;
+  if (ix.suffix16 != nullptr) {
+    // binary search of the needle's bucket [start, end) in its 2-byte suffixes
+    const uint16_t target = (uint16_t)(needle & ((1ull << ix.shift) - 1));
+    int64_t base = __ldg(ix.offsets + b);
+    const int64_t end = __ldg(ix.offsets + b + 1);
+    int64_t n = end - base;
+    if (n <= 0) return -1;
+    while (n > 1) {
+      const int64_t half = n >> 1;
+      base = (__ldg(ix.suffix16 + base + half) <= target) ? base + half : base;
+      n -= half;
+    }
+    return __ldg(ix.suffix16 + base) == target ? base : -1;
+  }
+  // a window of the largest bucket's length starting at the bucket, moved back to end at n
+  int64_t base = min((int64_t)__ldg(ix.offsets + b), ix.n_states - len);
   while (len > 1) {
     const int64_t half = len >> 1;
     base = (__ldg(ix.reps + base + half) < needle) ? base + half : base;
@@ -72,6 +88,7 @@ __device__ __forceinline__ DeviceIndex reload_index(const DeviceIndex* p) {
   r.norms = v->norms;
   r.inv_norms = v->inv_norms;
   r.offsets = v->offsets;
+  r.suffix16 = v->suffix16;
   r.shift = v->shift;
   r.range_size = v->range_size;
   r.prefix_bits = v->prefix_bits;
