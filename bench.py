@@ -40,7 +40,7 @@ if REPO not in sys.path:
 # DRAM bytes (read + write) of one matvec launch from an ncu capture of the same workload, with the
 # integer (ALU) pipe utilisation of that capture; summaries and commands in profiles/.
 NCU_CAPTURES = {
-    "j1j2_6x6": {"traffic": 102.806e9 + 1.102e9, "alu_pipe_pct": 70.5,
+    "j1j2_6x6": {"traffic": 34.214e9 + 0.265e9, "alu_pipe_pct": 68.7,
                  "source": "profiles/k_matvec_packed_j1j2_6x6.md"},
     "xxz24_sectors": {"traffic": 5.402e9 + 0.706e9, "alu_pipe_pct": 59.3, "fp64_pipe_pct": 20.9,
                       "source": "profiles/k_matvec_sectors_pairs_xxz24.md"},
