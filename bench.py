@@ -42,8 +42,8 @@ if REPO not in sys.path:
 NCU_CAPTURES = {
     "j1j2_6x6": {"traffic": 34.214e9 + 0.265e9, "alu_pipe_pct": 68.7,
                  "source": "profiles/k_matvec_packed_j1j2_6x6.md"},
-    "xxz24_sectors": {"traffic": 5.402e9 + 0.706e9, "alu_pipe_pct": 59.3, "fp64_pipe_pct": 20.9,
-                      "source": "profiles/k_matvec_sectors_pairs_xxz24.md"},
+    "xxz24_sectors": {"traffic": 2.749e9 + 0.681e9, "alu_pipe_pct": 26.0, "fp64_pipe_pct": 80.4,
+                      "source": "profiles/k_matvec_sectors_xxz24.md"},
 }
 
 CONFIGS = {
@@ -754,9 +754,11 @@ def run_sectors(args):
                      "alu_pipe_pct": NCU_CAPTURES.get(args.config, {}).get("alu_pipe_pct"),
                      "fp64_pipe_pct": NCU_CAPTURES.get(args.config, {}).get("fp64_pipe_pct"),
                      "peak_source": peak_kind, "bytes_per_launch": bytes_per_launch,
-                     "note": "issue-bound gather kernel (FP32-pair multiply-adds on small groups); frac is of "
-                             "algorithmic bytes with every gather counted from DRAM; traffic (ncu, batched "
-                             "launch) only for the workload captured whole"},
+                     "note": "FP64-pipe-bound gather kernel with 16 columns (FP32-pair multiply-adds are "
+                             "opt-in); frac is of algorithmic bytes with every gather counted from DRAM; "
+                             "traffic and pipe figures are from the ncu capture named in traffic_source "
+                             "(batched FP64 launch, N = 24), not measured by this run",
+                     "traffic_source": NCU_CAPTURES.get(args.config, {}).get("source")},
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_run * args.steps, "clocks": clocks.summary(),
         "basis_build_s": t_build,
         "extra": {"form": "one persistent launch over all sectors" if tune["batched"] else
