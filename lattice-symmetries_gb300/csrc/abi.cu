@@ -1245,9 +1245,16 @@ extern "C" void ls_chpl_matrix_vector_product(ls_hs_operator* matrix, int num_ve
     const size_t vbytes = (size_t)n * k * 8;
     // x is pinned for the copy when the system allows it (a DMA at full speed; a pageable copy of
     // a large host array can be staged far slower) and unpinned before returning
-    bool pinned_x = vbytes >= (1u << 20) &&
-                    cudaHostRegister((void*)x, vbytes, cudaHostRegisterReadOnly) == cudaSuccess;
-    if (!pinned_x) cudaGetLastError();  // not registered (already pinned, or unsupported): plain copy
+    bool pinned_x = false;
+    if (vbytes >= (1u << 20)) {
+      // the default flags need writable pages; read-only registration where those fail
+      pinned_x = cudaHostRegister((void*)x, vbytes, cudaHostRegisterDefault) == cudaSuccess;
+      if (!pinned_x) {
+        cudaGetLastError();
+        pinned_x = cudaHostRegister((void*)x, vbytes, cudaHostRegisterReadOnly) == cudaSuccess;
+      }
+      if (!pinned_x) cudaGetLastError();  // not registered (already pinned, or unsupported): plain copy
+    }
     const bool overlap = (const char*)y < (const char*)x + vbytes && (const char*)x < (const char*)y + vbytes;
     {
       StageScope stage("io.h2d", s);
