@@ -964,7 +964,7 @@ def main():
     # block matvec (16 right-hand sides) and adjoint, per vector
     extra = {} if args.no_extras else block_and_adjoint(op, rng, D, elements, ms_per_step, args.steps, x, y, sptr)
 
-    cpu, parity = None, None
+    cpu, parity, cpu_enum = None, None, None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         O = _oracle()
@@ -979,6 +979,19 @@ def main():
                "sample": "5 seeded random samples of {} of {} columns (oracle/ls_oracle.c lso_matvec_sample: "
                          "Benes orbit scan, prefix index, atomic scatter), {:.2f} s each".format(cols, D, t_s)}
         parity = check_parity(sampler, op, D, x_host, args.config, states)
+        # the reference's enumeration (StatesEnumeration.chpl:242-268) restated on the host cores,
+        # over the whole sector, against the GPU build
+        lo, hi = basis._estimates()
+        t0 = time.perf_counter()
+        cpu_reps = O.enumerate_projected_par(g, lo, hi, lane_width=8, use_benes=True)
+        t_cpu_enum = time.perf_counter() - t0
+        n_cand = O.rank(hi) - O.rank(lo) + 1
+        cpu_enum = {"candidates": n_cand, "seconds": t_cpu_enum, "candidates_per_s": n_cand / t_cpu_enum,
+                    "cores": threads, "gpu_seconds": t_build, "gpu_speedup": t_cpu_enum / t_build,
+                    "how": "oracle/ls_oracle.c lso_enumerate_projected_par (Benes orbit scan, chunk order "
+                           "with early exit), all host threads"}
+        parity["enumeration_equals_cpu"] = bool(np.array_equal(cpu_reps, states))
+        del cpu_reps
 
     if rank == 0:
         line = {
@@ -997,7 +1010,7 @@ def main():
                                  "not measured by this run"},
             "nnz": nnz,
             "cpu_baseline": cpu, "parity": parity, "e2e": e2e, "gpu_launches": 2 * args.steps,
-            "clocks": clocks.summary(), "basis_build_s": t_build, "extra": extra,
+            "clocks": clocks.summary(), "basis_build_s": t_build, "cpu_enumeration": cpu_enum, "extra": extra,
             "stages_ms": {"basis_build": {k: v[1] for k, v in stages_build.items()},
                           "matvec_step": {k: v[1] for k, v in stages_step.items()},
                           "how": "CUDA events per stage (ls_gpu_set_tracing), untimed passes"},
