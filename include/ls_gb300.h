@@ -500,6 +500,19 @@ int ls_gpu_block_gram(int64_t S, int64_t D, int k, double const *d_x, double con
 int ls_gpu_block_update(int64_t S, int64_t D, int k, double beta, double const *d_w,
                         double const *d_x1, double const *d_m1, double const *d_x2,
                         double const *d_m2, double *d_out, void *stream);
+/* The block update on the tensor cores (same arguments and aliasing rules as
+ * ls_gpu_block_update).  Each row of [X1 | X2] and each column of [M1; M2] (as real matrices) is
+ * put in a fixed-point frame above its largest magnitude and cut into eight 7-bit digits (exact
+ * bf16 values); tcgen05 MMAs sum the digit products of equal weight exactly in FP32, and the
+ * eight weight groups of an output are combined in 64-bit integers and rounded once to FP64
+ * before beta W is added in FP64.  Each output is within about (4k + 2) 2^-54 2^(E_r + E_c) of
+ * the exact value, where 2^E_r and 2^E_c (< 2x the largest magnitudes) are the row's and the
+ * column's frames: the error bound of an FP64 dot product of the same length.  Inputs must be
+ * finite.  Stream-ordered (one cudaMallocAsync for the digit image of M); a wait that times out
+ * inside the kernel is reported as LS_GPU_ERR_CUDA by the next matvec call. */
+int ls_gpu_block_update_tc(int64_t S, int64_t D, int k, double beta, double const *d_w,
+                           double const *d_x1, double const *d_m1, double const *d_x2,
+                           double const *d_m2, double *d_out, void *stream);
 
 #if defined(__cplusplus)
 } /* extern "C" */

@@ -1182,6 +1182,8 @@ int read_and_clear_error(cudaStream_t s) {
     return fail(LS_GPU_ERR_BASIS,
                 "a generated basis state does not belong to the basis (the operator does not conserve "
                 "the basis' particle numbers)");
+  if (h[1] != 0)
+    return fail(LS_GPU_ERR_CUDA, "a tensor-core block product gave up waiting for its MMAs (results invalid)");
   return 0;
 }
 

@@ -269,5 +269,9 @@ int launch_block_gram(int64_t S, int64_t D, int k, const double* d_x, const doub
 int launch_block_update(int64_t S, int64_t D, int k, double beta, const double* d_w, const double* d_x1,
                         const double* d_m1, const double* d_x2, const double* d_m2, double* d_out,
                         cudaStream_t s);
+// tensor-core form (blockops_tc.cu): same contract as launch_block_update
+int launch_block_update_tc(int64_t S, int64_t D, int k, double beta, const double* d_w, const double* d_x1,
+                           const double* d_m1, const double* d_x2, const double* d_m2, double* d_out,
+                           cudaStream_t s);
 
 }  // namespace lsg

@@ -31,16 +31,24 @@ from typing import Callable, List, Optional, Tuple
 import numpy as np
 
 
+DENSE_MODES = ("tensor", "paired", "fp64")
 DENSE_DEFAULT = "paired"
 
 
-def _paired(X, dense) -> bool:
+def _mode(X, dense) -> str:
+    """The dense-product arithmetic for block X: 'tensor' / 'paired' (the library's kernels) need
+    a CUDA complex128 [S, D, k] block with k <= 16, else torch FP64 GEMMs run."""
     import torch
 
     mode = DENSE_DEFAULT if dense is None else dense
-    if mode not in ("paired", "fp64"):
-        raise ValueError("dense must be 'paired' or 'fp64'")
-    return mode == "paired" and X.is_cuda and X.dtype == torch.complex128 and X.dim() == 3 and X.shape[-1] <= 16
+    if mode not in DENSE_MODES:
+        raise ValueError("dense must be one of " + ", ".join(repr(m) for m in DENSE_MODES))
+    native = X.is_cuda and X.dtype == torch.complex128 and X.dim() == 3 and X.shape[-1] <= 16
+    return mode if native else "fp64"
+
+
+def _paired(X, dense) -> bool:
+    return _mode(X, dense) != "fp64"
 
 
 def _native():
@@ -81,7 +89,8 @@ def _gram(X, Y, dense=None, blocks: int = 256, min_rows: int = 64):
 
 def _update(out, beta: float, W, X1, M1, X2=None, M2=None, dense=None):
     """out = beta W + X1 M1 (+ X2 M2) for [S, D, k] blocks and [S, k, k] matrices; out may be W, X1
-    or X2 (paired: one call of ls_gpu_block_update; fp64: torch GEMMs)."""
+    or X2 (tensor: one call of ls_gpu_block_update_tc; paired: ls_gpu_block_update; fp64: torch
+    GEMMs)."""
     import torch
 
     S, D, k = X1.shape
@@ -95,9 +104,10 @@ def _update(out, beta: float, W, X1, M1, X2=None, M2=None, dense=None):
         if W is not None and beta != 0.0:
             W = W.contiguous()
         stream = torch.cuda.current_stream(X1.device).cuda_stream
-        rc = lib.ls_gpu_block_update(S, D, k, float(beta), W.data_ptr() if (W is not None and beta != 0.0) else None,
-                                     X1.data_ptr(), M1.data_ptr(), X2.data_ptr() if X2 is not None else None,
-                                     M2.data_ptr() if M2 is not None else None, out.data_ptr(), stream)
+        fn = lib.ls_gpu_block_update_tc if _mode(X1, dense) == "tensor" else lib.ls_gpu_block_update
+        rc = fn(S, D, k, float(beta), W.data_ptr() if (W is not None and beta != 0.0) else None,
+                X1.data_ptr(), M1.data_ptr(), X2.data_ptr() if X2 is not None else None,
+                M2.data_ptr() if M2 is not None else None, out.data_ptr(), stream)
         N.check(rc, "block update")
         return out
     if beta != 0.0 and out is W and X1 is not out and X2 is not out:
