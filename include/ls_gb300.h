@@ -500,6 +500,17 @@ int ls_gpu_block_gram(int64_t S, int64_t D, int k, double const *d_x, double con
 int ls_gpu_block_update(int64_t S, int64_t D, int k, double beta, double const *d_w,
                         double const *d_x1, double const *d_m1, double const *d_x2,
                         double const *d_m2, double *d_out, void *stream);
+/* The Gram matrices on the tensor cores (same arguments as ls_gpu_block_gram).  Per tile of 128
+ * rows every complex column of X and of Y gets a fixed-point frame above its largest magnitude in
+ * the tile; values are cut into eight 7-bit digits (exact bf16), tcgen05 MMAs sum the digit
+ * products of equal weight exactly in FP32, and each tile's sums are joined in 64-bit integers,
+ * converted to FP64 once and accumulated in FP64 (per-CTA partials added in a fixed order:
+ * deterministic).  Each tile adds an error below about 2^-46 2^(E_x + E_y) per entry (128 rows of
+ * FP64-exact digit products truncated at weight 2^-56 of the frames 2^E, which are below twice
+ * the tile's largest magnitudes), the size of an FP64 dot product's rounding error over the tile.
+ * Inputs must be finite.  Stream-ordered (cudaMallocAsync / cudaMemsetAsync of the partials). */
+int ls_gpu_block_gram_tc(int64_t S, int64_t D, int k, double const *d_x, double const *d_y,
+                         double *d_g, void *stream);
 /* The block update on the tensor cores (same arguments and aliasing rules as
  * ls_gpu_block_update).  Each row of [X1 | X2] and each column of [M1; M2] (as real matrices) is
  * put in a fixed-point frame above its largest magnitude and cut into eight 7-bit digits (exact

@@ -193,6 +193,7 @@ _SIGNATURES = [
     ("ls_gpu_block_gram", c_int, [c_int64, c_int64, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("ls_gpu_block_update", c_int, [c_int64, c_int64, c_int, c_double, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_void_p, c_void_p]),
+    ("ls_gpu_block_gram_tc", c_int, [c_int64, c_int64, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("ls_gpu_block_update_tc", c_int, [c_int64, c_int64, c_int, c_double, c_void_p, c_void_p, c_void_p,
                                        c_void_p, c_void_p, c_void_p, c_void_p]),
 ]

@@ -254,6 +254,11 @@ int launch_block_gram(int64_t S, int64_t D, int k, const double* d_x, const doub
   return ok ? 0 : LS_GPU_ERR_CUDA;
 }
 
+int launch_gram_partial_sum(const double2* partial, int chunks, int nout, int64_t S, double2* G, cudaStream_t s) {
+  k_block_gram_sum<<<dim3((unsigned)S, (unsigned)((nout + 31) / 32)), 1024, 0, s>>>(partial, chunks, nout, G);
+  return cuda_ok(cudaGetLastError(), "k_block_gram_sum") ? 0 : LS_GPU_ERR_CUDA;
+}
+
 int launch_block_update(int64_t S, int64_t D, int k, double beta, const double* d_w, const double* d_x1,
                         const double* d_m1, const double* d_x2, const double* d_m2, double* d_out,
                         cudaStream_t s) {

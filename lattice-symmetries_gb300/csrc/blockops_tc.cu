@@ -45,7 +45,9 @@ namespace {
 
 constexpr int kDigits = 8;
 constexpr int kRows = 128;  // rows per tile: the MMA's M
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;  // 16 warps: 4 per SM sub-partition
+constexpr int kWarps = kThreads / 32;
+constexpr int kParts = kThreads / 128;  // epilogue: column parts per lane quarter
 constexpr uint32_t kRowCore = 128;      // bytes between core matrices adjacent in rows
 constexpr long long kWaitCycles = 4000000000ll;  // about 2 s at GB300 clocks
 
@@ -174,7 +176,7 @@ template <int KP>
 struct UpdTile {
   static constexpr int G = UpdShape<KP>::G;
   static constexpr int RPW = 32 / G;               // rows per warp and pass
-  static constexpr int PASSES = kRows * G / kThreads;  // 4 (kp = 16) or 2 (kp = 8)
+  static constexpr int PASSES = kRows * G / kThreads;  // 2 (kp = 16) or 1 (kp = 8)
   double2 v[PASSES][4];                            // this thread's 8 reals per pass
 };
 
@@ -188,7 +190,7 @@ __device__ __forceinline__ void update_load(UpdTile<KP>& t, int64_t tile_row0, i
   const int c0 = (g % (T::G / 2)) * 4;
 #pragma unroll
   for (int p = 0; p < T::PASSES; ++p) {
-    const int r = (p * 8 + warp) * T::RPW + lane / T::G;
+    const int r = (p * kWarps + warp) * T::RPW + lane / T::G;
     const int64_t row = tile_row0 + r;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -206,7 +208,7 @@ __device__ __forceinline__ void update_produce(const UpdTile<KP>& t, uint8_t* A,
   const int g = lane % T::G;
 #pragma unroll
   for (int p = 0; p < T::PASSES; ++p) {
-    const int r = (p * 8 + warp) * T::RPW + lane / T::G;
+    const int r = (p * kWarps + warp) * T::RPW + lane / T::G;
     int e = 0;
 #pragma unroll
     for (int q = 0; q < 4; ++q) e = max(e, max(exp_field(t.v[p][q].x), exp_field(t.v[p][q].y)));
@@ -217,8 +219,9 @@ __device__ __forceinline__ void update_produce(const UpdTile<KP>& t, uint8_t* A,
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       uint32_t br[kDigits], bi[kDigits];
-      digits8(fixed56(t.v[p][q].x, e), t.v[p][q].x < 0.0, br);
-      digits8(fixed56(t.v[p][q].y, e), t.v[p][q].y < 0.0, bi);
+      // signs from the high words (integer test: no FP64 comparison)
+      digits8(fixed56(t.v[p][q].x, e), __double2hiint(t.v[p][q].x) < 0, br);
+      digits8(fixed56(t.v[p][q].y, e), __double2hiint(t.v[p][q].y) < 0, bi);
 #pragma unroll
       for (int j = 0; j < kDigits; ++j) w[j][q] = __byte_perm(br[j], bi[j], 0x7632);
     }
@@ -237,40 +240,47 @@ __device__ __forceinline__ void update_epilogue(uint32_t tmem_buf, const int* ro
                                                 const double2* W, double2* out) {
   using Sh = UpdShape<KP>;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int quarter = warp & 3, half = warp >> 2;
+  const int quarter = warp & 3, part = warp >> 2;
+  constexpr int RC = Sh::NC / kParts;  // real columns of this thread
+  constexpr int KC = RC / 2;           // complex columns
   const int r = quarter * 32 + lane;
   const int64_t row = tile_row0 + r;
-  const uint32_t taddr = tmem_buf + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(half * KP);
-  long long H[KP];
-  uint32_t a[KP];
-  // group 0 .. 6: Horner in base 2^7
+  const uint32_t taddr = tmem_buf + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(part * RC);
+  // W's part of this row first, so that its latency overlaps the tensor-memory loads and the
+  // integer combination
+  const int j0 = part * KC;
+  const bool live = row < D;
+  double2 w[KC];
+#pragma unroll
+  for (int c = 0; c < KC; ++c)
+    w[c] = (beta != 0.0 && live && j0 + c < k) ? W[(sec_base + row) * k + j0 + c] : make_double2(0.0, 0.0);
+  long long H[RC];
+  uint32_t a[RC];
+  // groups 0 .. 6: Horner in base 2^7
 #pragma unroll
   for (int t = 0; t < kDigits; ++t) {
-    if constexpr (KP == 16) tc::tmem_ld16(taddr + t * Sh::NC, a);
-    else tc::tmem_ld8(taddr + t * Sh::NC, a);
+    tc::tmem_ld<RC>(taddr + t * Sh::NC, a);
     tc::tmem_ld_wait();
 #pragma unroll
-    for (int c = 0; c < KP; ++c) {
+    for (int c = 0; c < RC; ++c) {
       const long long g = (long long)__float2int_rn(__uint_as_float(a[c]));
       if (t == 0) H[c] = g;
       else if (t < kDigits - 1) H[c] = H[c] * 128 + g;
       else H[c] += g >> 7;  // group 7, truncated to the unit of group 6
     }
   }
-  if (row >= D) return;
+  if (!live) return;
   const int er = rowexp[r];
-  const double2* wrow = W != nullptr ? W + (sec_base + row) * k : nullptr;
   double2* orow = out + (sec_base + row) * k;
 #pragma unroll
-  for (int c = 0; c < KP; c += 2) {
-    const int j = (half * KP + c) >> 1;  // complex column
+  for (int c = 0; c < KC; ++c) {
+    const int j = j0 + c;  // complex column
     if (j >= k) break;
-    double re = int64_scaled_to_double(H[c], er + colexp[half * KP + c] - 2100);
-    double im = int64_scaled_to_double(H[c + 1], er + colexp[half * KP + c + 1] - 2100);
+    double re = int64_scaled_to_double(H[2 * c], er + colexp[2 * j] - 2100);
+    double im = int64_scaled_to_double(H[2 * c + 1], er + colexp[2 * j + 1] - 2100);
     if (beta != 0.0) {
-      const double2 w = wrow[j];
-      re = fma(beta, w.x, re);
-      im = fma(beta, w.y, im);
+      re = fma(beta, w[c].x, re);
+      im = fma(beta, w[c].y, im);
     }
     orow[j] = make_double2(re, im);
   }
@@ -421,6 +431,306 @@ int run_update_tc(int64_t S, int64_t D, int k, double beta, const double* d_w, c
   return ok ? 0 : LS_GPU_ERR_CUDA;
 }
 
+// ---- the Gram kernel --------------------------------------------------------------------------
+//
+//     G[s] = X[s]^H Y[s]      (the contraction runs over the D rows)
+//
+// A tile of 128 rows is the K extent of one round of MMAs (8 K steps of 16 rows).  Every complex
+// column of X and of Y gets a frame over the tile's rows (its re and im parts share it, so that
+// the complex combination stays exact), and the digit planes are written transposed: element
+// (plane * NR + c, row) of a K-major operand, NR = 2 kp real columns.  One MMA with M = 128 covers
+// Q = 128 / NR consecutive planes of X; with the planes stacked in order behind Q - 1 zero planes,
+// lane block q of accumulator region rho collects exactly the products of weight t = rho Q + q:
+// for each plane j of Y, MMA(A = X planes rho Q - j .. rho Q - j + Q - 1, B = Y plane j) adds the
+// digit pairs (rho Q + q - j, j).  A cell sums at most 8 pairs x 128 rows of digit products,
+// |cell| <= 128 * 2^16 = 2^23 (exact in FP32).  After a tile the epilogue joins a lane's regions
+// into one 64-bit integer per column, converts it to FP64 with the tile's frames and adds it to
+// per-thread FP64 sums; at the end of a sector's rows the sums are reduced over lane blocks and
+// complex pairs into this CTA's partial Gram, and the partials are added over CTAs in a fixed
+// order by a second kernel (deterministic).
+
+template <int KP>
+struct GramShape {
+  static constexpr int NR = 2 * KP;      // real columns
+  static constexpr int Q = kRows / NR;   // digit planes per MMA: 4 (kp = 16) or 8 (kp = 8)
+  static constexpr int REG = kDigits / Q;  // accumulator regions: 2 or 1
+  static constexpr int Z = Q - 1;          // zero planes in front of X's planes
+  static constexpr int x_rows = (Z + kDigits) * NR;
+  static constexpr int y_rows = kDigits * NR;
+  static constexpr uint32_t x_kstride = x_rows * 16;
+  static constexpr uint32_t y_kstride = y_rows * 16;
+  static constexpr uint32_t x_bytes = (kRows / 8) * x_kstride;
+  static constexpr uint32_t y_bytes = (kRows / 8) * y_kstride;
+  static constexpr uint32_t p_bytes = kRows * NR * 8;  // flush buffer: 128 lanes x NR doubles
+  static constexpr uint32_t smem = x_bytes + y_bytes + p_bytes;
+  static constexpr uint32_t buf_cols = REG * NR;       // tensor-memory columns per tile
+  static constexpr uint32_t tmem_cols = 2 * buf_cols < 32 ? 32 : 2 * buf_cols;
+  static constexpr int units = NR * (kRows / 8);       // (column, 8-row group) units per operand
+  static constexpr int PASSES = 2 * units / kThreads;  // units of X and Y per thread
+  static constexpr int DC = NR / kParts;               // epilogue: columns of Y per thread
+};
+
+template <int KP>
+struct GramTile {
+  double v[GramShape<KP>::PASSES][8];
+};
+
+template <int KP>
+__device__ __forceinline__ void gram_load(GramTile<KP>& t, int64_t row0, int64_t D, int k, int64_t sec_base,
+                                          const double* X, const double* Y, bool same) {
+  using Sh = GramShape<KP>;
+#pragma unroll
+  for (int p = 0; p < Sh::PASSES; ++p) {
+    const int u = threadIdx.x + p * kThreads;
+    const int which = u / Sh::units, v = u % Sh::units;
+    const int c = v % Sh::NR, g = v / Sh::NR;
+    const double* P = which == 0 ? X : Y;
+    const bool active = !(same && which == 1) && c < 2 * k;
+#pragma unroll
+    for (int rr = 0; rr < 8; ++rr) {
+      const int64_t row = row0 + 8 * g + rr;
+      t.v[p][rr] = (active && row < D) ? P[((sec_base + row) * k) * 2 + c] : 0.0;
+    }
+  }
+}
+
+// Frames (per complex column, into colmax[2][16] by atomicMax), then the digit planes.
+template <int KP>
+__device__ __forceinline__ void gram_produce(const GramTile<KP>& t, uint8_t* XD, uint8_t* YD, int (*colmax)[16],
+                                             bool same) {
+  using Sh = GramShape<KP>;
+#pragma unroll
+  for (int p = 0; p < Sh::PASSES; ++p) {
+    const int u = threadIdx.x + p * kThreads;
+    const int which = u / Sh::units, c = (u % Sh::units) % Sh::NR;
+    int e = 0;
+#pragma unroll
+    for (int rr = 0; rr < 8; ++rr) e = max(e, exp_field(t.v[p][rr]));
+    e = max(e, __shfl_xor_sync(0xffffffffu, e, 1));  // re and im of one complex column
+    if (!(same && which == 1) && (c & 1) == 0 && e > 0) atomicMax(&colmax[which][c >> 1], e);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int p = 0; p < Sh::PASSES; ++p) {
+    const int u = threadIdx.x + p * kThreads;
+    const int which = u / Sh::units, v = u % Sh::units;
+    const int c = v % Sh::NR, g = v / Sh::NR;
+    if (same && which == 1) continue;
+    const int e = colmax[which][c >> 1];
+    uint32_t w[kDigits][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint32_t b0[kDigits], b1[kDigits];
+      const double x0 = t.v[p][2 * q], x1 = t.v[p][2 * q + 1];
+      digits8(fixed56(x0, e), __double2hiint(x0) < 0, b0);
+      digits8(fixed56(x1, e), __double2hiint(x1) < 0, b1);
+#pragma unroll
+      for (int j = 0; j < kDigits; ++j) w[j][q] = __byte_perm(b0[j], b1[j], 0x7632);
+    }
+    uint8_t* base = which == 0 ? XD : YD;
+    const uint32_t ks = which == 0 ? Sh::x_kstride : Sh::y_kstride;
+    const int plane0 = which == 0 ? Sh::Z : 0;
+#pragma unroll
+    for (int j = 0; j < kDigits; ++j) {
+      const int m = (plane0 + j) * Sh::NR + c;
+      *reinterpret_cast<uint4*>(base + g * ks + (m >> 3) * kRowCore + (m & 7) * 16) =
+          make_uint4(w[j][0], w[j][1], w[j][2], w[j][3]);
+    }
+  }
+}
+
+// Adds one finished tile to the per-thread FP64 sums acc[d] (this thread: lane (quarter, lane),
+// i.e. lane block q = lane / NR and column c = lane % NR of X; columns d of Y in its part).
+template <int KP>
+__device__ __forceinline__ void gram_epilogue(uint32_t tmem_buf, const int (*colmax)[16], bool same,
+                                              double (&acc)[GramShape<KP>::DC]) {
+  using Sh = GramShape<KP>;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int quarter = warp & 3, part = warp >> 2;
+  const int l = quarter * 32 + lane;
+  const int q = l / Sh::NR, c = l % Sh::NR;
+  const uint32_t taddr = tmem_buf + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(part * Sh::DC);
+  uint32_t cell[Sh::REG][Sh::DC];
+#pragma unroll
+  for (int rho = 0; rho < Sh::REG; ++rho) tc::tmem_ld<Sh::DC>(taddr + rho * Sh::NR, cell[rho]);
+  tc::tmem_ld_wait();
+  const int ec = colmax[0][c >> 1];
+  const int* ey = colmax[same ? 0 : 1];
+#pragma unroll
+  for (int dd = 0; dd < Sh::DC; ++dd) {
+    long long v = 0;
+#pragma unroll
+    for (int rho = 0; rho < Sh::REG; ++rho) v = v * (1ll << (7 * Sh::Q)) + (long long)__float2int_rn(__uint_as_float(cell[rho][dd]));
+    const int ed = ey[(part * Sh::DC + dd) >> 1];
+    // v counts units of 2^(E_c + E_d - 14 - 7 q - 7 Q (REG - 1)), E = biased exponent - 1022
+    acc[dd] += int64_scaled_to_double(v, ec + ed - 2058 - 7 * q - 7 * Sh::Q * (Sh::REG - 1));
+  }
+}
+
+// Reduces the per-thread sums over lane blocks and complex pairs into partial[s][blockIdx.x]
+// (k x k complex), then clears them.
+template <int KP>
+__device__ __forceinline__ void gram_flush(double (&acc)[GramShape<KP>::DC], double* P, int k, int64_t s,
+                                           double2* partial) {
+  using Sh = GramShape<KP>;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int quarter = warp & 3, part = warp >> 2;
+  const int l = quarter * 32 + lane;
+#pragma unroll
+  for (int dd = 0; dd < Sh::DC; ++dd) {
+    P[l * Sh::NR + part * Sh::DC + dd] = acc[dd];
+    acc[dd] = 0.0;
+  }
+  __syncthreads();
+  const int nout = k * k;
+  for (int o = threadIdx.x; o < nout; o += kThreads) {
+    const int a = o / k, b = o % k;
+    double re = 0.0, im = 0.0;
+    for (int q = 0; q < Sh::Q; ++q) {
+      const double* Pq = P + (size_t)q * Sh::NR * Sh::NR;
+      // conj(x) y = (xr yr + xi yi) + i (xr yi - xi yr)
+      re += Pq[(2 * a) * Sh::NR + 2 * b] + Pq[(2 * a + 1) * Sh::NR + 2 * b + 1];
+      im += Pq[(2 * a) * Sh::NR + 2 * b + 1] - Pq[(2 * a + 1) * Sh::NR + 2 * b];
+    }
+    partial[((size_t)s * gridDim.x + blockIdx.x) * nout + o] = make_double2(re, im);
+  }
+  __syncthreads();
+}
+
+template <int KP>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_block_gram_tc(int64_t D, int k, int64_t tiles_per_sector, int64_t total_tiles, const double* X,
+                    const double* Y, bool same, double2* partial, int* err) {
+  using Sh = GramShape<KP>;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* XD = smem;
+  uint8_t* YD = smem + Sh::x_bytes;
+  double* P = reinterpret_cast<double*>(smem + Sh::x_bytes + Sh::y_bytes);
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int colmax[3][2][16];  // frames of three tiles in flight (reset one tile ahead)
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int64_t t_begin = (int64_t)blockIdx.x * total_tiles / gridDim.x;
+  const int64_t t_end = (int64_t)(blockIdx.x + 1) * total_tiles / gridDim.x;
+  // zero planes of X (never written again)
+  for (uint32_t g = 0; g < kRows / 8; ++g)
+    for (uint32_t e = tid; e < (uint32_t)(Sh::Z * Sh::NR * 16 / 16); e += kThreads)
+      reinterpret_cast<uint4*>(XD + g * Sh::x_kstride)[e] = make_uint4(0, 0, 0, 0);
+  if (tid < 3 * 2 * 16) (&colmax[0][0][0])[tid] = 0;
+  if (warp == 0) {
+    tc::tmem_alloc(tc::smem_u32(&tmem_slot), Sh::tmem_cols);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(tc::smem_u32(&mbar[0]), 1);
+    tc::mbar_init(tc::smem_u32(&mbar[1]), 1);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t x0 = tc::smem_u32(XD), y0 = same ? x0 + (Sh::Z * Sh::NR / 8) * kRowCore : tc::smem_u32(YD);
+  const uint32_t yks = same ? Sh::x_kstride : Sh::y_kstride;
+  double acc[Sh::DC];
+#pragma unroll
+  for (int dd = 0; dd < Sh::DC; ++dd) acc[dd] = 0.0;
+  bool failed = false;
+  GramTile<KP> regs;
+  if (t_begin < t_end)
+    gram_load<KP>(regs, (t_begin % tiles_per_sector) * kRows, D, k, (t_begin / tiles_per_sector) * D, X, Y, same);
+  for (int64_t tile = t_begin; tile < t_end; ++tile) {
+    const int it = (int)(tile - t_begin);
+    const int buf = it & 1;
+    const int64_t s = tile / tiles_per_sector;
+    if (it >= 1) {
+      const bool ok = tc::mbar_wait(tc::smem_u32(&mbar[buf ^ 1]), ((it - 1) >> 1) & 1, kWaitCycles);
+      if (__syncthreads_or(!ok)) {
+        failed = true;
+        break;
+      }
+      tc::fence_after_sync();
+    }
+    gram_produce<KP>(regs, XD, YD, colmax[it % 3], same);
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0) {
+      const uint32_t d0 = tmem + buf * Sh::buf_cols;
+#pragma unroll 1
+      for (int ks = 0; ks < kRows / 16; ++ks) {
+#pragma unroll
+        for (int rho = 0; rho < Sh::REG; ++rho) {
+          const int jmax = min(kDigits - 1, rho * Sh::Q + Sh::Q - 1);
+          for (int j = 0; j <= jmax; ++j) {
+            const uint32_t arow = (uint32_t)(Sh::Z + rho * Sh::Q - j) * Sh::NR;
+            const uint64_t ad =
+                tc::smem_desc(x0 + (arow / 8) * kRowCore + ks * 2 * Sh::x_kstride, Sh::x_kstride, kRowCore);
+            const uint64_t bd =
+                tc::smem_desc(y0 + (uint32_t)(j * Sh::NR / 8) * kRowCore + ks * 2 * yks, yks, kRowCore);
+            tc::mma_bf16(d0 + rho * Sh::NR, ad, bd, tc::idesc_bf16_f32(kRows, Sh::NR), (ks > 0 || j > 0) ? 1u : 0u);
+          }
+        }
+      }
+      tc::commit(tc::smem_u32(&mbar[buf]));
+    }
+    if (tid < 2 * 16) (&colmax[(it + 1) % 3][0][0])[tid] = 0;  // frames of the next tile
+    if (tile + 1 < t_end)
+      gram_load<KP>(regs, ((tile + 1) % tiles_per_sector) * kRows, D, k, ((tile + 1) / tiles_per_sector) * D, X, Y,
+                    same);
+    if (it >= 1) {
+      gram_epilogue<KP>(tmem + (buf ^ 1) * Sh::buf_cols, colmax[(it - 1) % 3], same, acc);
+      if ((tile - 1) / tiles_per_sector != s) gram_flush<KP>(acc, P, k, (tile - 1) / tiles_per_sector, partial);
+    }
+    tc::fence_before_sync();
+  }
+  const int n = (int)(t_end - t_begin);
+  if (!failed && n >= 1) {
+    const int lb = (n - 1) & 1;
+    const bool ok = tc::mbar_wait(tc::smem_u32(&mbar[lb]), ((n - 1) >> 1) & 1, kWaitCycles);
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+    } else {
+      tc::fence_after_sync();
+      gram_epilogue<KP>(tmem + lb * Sh::buf_cols, colmax[(n - 1) % 3], same, acc);
+      gram_flush<KP>(acc, P, k, (t_end - 1) / tiles_per_sector, partial);
+    }
+  }
+  if (failed && threadIdx.x == 0) atomicExch(err, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, Sh::tmem_cols);
+}
+
+template <int KP>
+int run_gram_tc(int64_t S, int64_t D, int k, const double* d_x, const double* d_y, double* d_g, cudaStream_t st) {
+  using Sh = GramShape<KP>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    if (!cuda_ok(cudaFuncSetAttribute(k_block_gram_tc<KP>, cudaFuncAttributeMaxDynamicSharedMemorySize, Sh::smem),
+                 "cudaFuncSetAttribute(k_block_gram_tc)"))
+      return LS_GPU_ERR_CUDA;
+    attr_set = true;
+  }
+  const int64_t tiles_per_sector = (D + kRows - 1) / kRows;
+  const int64_t total = S * tiles_per_sector;
+  const int grid = (int)std::min<int64_t>(total, (int64_t)num_sms());
+  const int nout = k * k;
+  const size_t pbytes = (size_t)S * grid * nout * sizeof(double2);
+  double2* partial = nullptr;
+  if (!cuda_ok(cudaMallocAsync((void**)&partial, pbytes, st), "cudaMallocAsync(Gram partials)")) return LS_GPU_ERR_CUDA;
+  // a CTA writes the partials of the sectors its rows touch; the others stay zero
+  bool ok = cuda_ok(cudaMemsetAsync(partial, 0, pbytes, st), "cudaMemsetAsync(Gram partials)");
+  if (ok) {
+    k_block_gram_tc<KP><<<grid, kThreads, Sh::smem, st>>>(D, k, tiles_per_sector, total, d_x, d_y, d_x == d_y,
+                                                          partial, device_error_word() + 1);
+    ok = cuda_ok(cudaGetLastError(), "k_block_gram_tc");
+  }
+  if (ok) ok = launch_gram_partial_sum(partial, grid, nout, S, reinterpret_cast<double2*>(d_g), st) == 0;
+  ok = cuda_ok(cudaFreeAsync(partial, st), "cudaFreeAsync(Gram partials)") && ok;
+  return ok ? 0 : LS_GPU_ERR_CUDA;
+}
+
 }  // namespace
 
 int launch_block_update_tc(int64_t S, int64_t D, int k, double beta, const double* d_w, const double* d_x1,
@@ -437,7 +747,24 @@ int launch_block_update_tc(int64_t S, int64_t D, int k, double beta, const doubl
                 : run_update_tc<16>(S, D, k, beta, d_w, d_x1, d_m1, d_x2, d_m2, d_out, s);
 }
 
+int launch_block_gram_tc(int64_t S, int64_t D, int k, const double* d_x, const double* d_y, double* d_g,
+                         cudaStream_t s) {
+  if (S < 1 || S > 65535 || D < 0 || k < 1 || k > 16)
+    return fail(LS_GPU_ERR_INVALID, "block Gram: need 1 <= S <= 65535, D >= 0, 1 <= k <= 16");
+  if (d_g == nullptr || (D > 0 && (d_x == nullptr || d_y == nullptr)))
+    return fail(LS_GPU_ERR_INVALID, "block Gram: NULL pointer");
+  if (D == 0)
+    return cuda_ok(cudaMemsetAsync(d_g, 0, (size_t)S * k * k * 16, s), "block Gram (empty)") ? 0 : LS_GPU_ERR_CUDA;
+  StageScope stage("lanczos.gram", s);
+  return k <= 8 ? run_gram_tc<8>(S, D, k, d_x, d_y, d_g, s) : run_gram_tc<16>(S, D, k, d_x, d_y, d_g, s);
+}
+
 }  // namespace lsg
+
+extern "C" int ls_gpu_block_gram_tc(int64_t S, int64_t D, int k, double const* d_x, double const* d_y, double* d_g,
+                                    void* stream) {
+  return lsg::launch_block_gram_tc(S, D, k, d_x, d_y, d_g, (cudaStream_t)stream);
+}
 
 extern "C" int ls_gpu_block_update_tc(int64_t S, int64_t D, int k, double beta, double const* d_w,
                                       double const* d_x1, double const* d_m1, double const* d_x2,

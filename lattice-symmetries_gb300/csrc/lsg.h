@@ -269,7 +269,11 @@ int launch_block_gram(int64_t S, int64_t D, int k, const double* d_x, const doub
 int launch_block_update(int64_t S, int64_t D, int k, double beta, const double* d_w, const double* d_x1,
                         const double* d_m1, const double* d_x2, const double* d_m2, double* d_out,
                         cudaStream_t s);
-// tensor-core form (blockops_tc.cu): same contract as launch_block_update
+// G[s][o] = sum over c < chunks of partial[s][c][o] (o < nout), in a fixed order (blockops.cu)
+int launch_gram_partial_sum(const double2* partial, int chunks, int nout, int64_t S, double2* G, cudaStream_t s);
+// tensor-core forms (blockops_tc.cu): same contracts as launch_block_gram / launch_block_update
+int launch_block_gram_tc(int64_t S, int64_t D, int k, const double* d_x, const double* d_y, double* d_g,
+                         cudaStream_t s);
 int launch_block_update_tc(int64_t S, int64_t D, int k, double beta, const double* d_w, const double* d_x1,
                            const double* d_m1, const double* d_x2, const double* d_m2, double* d_out,
                            cudaStream_t s);

@@ -60,7 +60,7 @@ def _native():
 def _gram(X, Y, dense=None, blocks: int = 256, min_rows: int = 64):
     """X^H Y for [S, D, k] blocks as [S, k, k].
 
-    paired: one call of ls_gpu_block_gram.  fp64 (torch): a single GEMM with inner dimension D
+    tensor: one call of ls_gpu_block_gram_tc; paired: ls_gpu_block_gram.  fp64 (torch): a single GEMM with inner dimension D
     (hundreds of thousands) and a 16 x 16 output leaves most of the GPU idle, so the rows are split
     into `blocks` equal row blocks (S * blocks GEMMs whose partial results are summed) plus the
     remaining D mod blocks rows."""
@@ -73,7 +73,8 @@ def _gram(X, Y, dense=None, blocks: int = 256, min_rows: int = 64):
         Y = Y.contiguous()
         G = torch.empty((S, k, k), dtype=X.dtype, device=X.device)
         stream = torch.cuda.current_stream(X.device).cuda_stream
-        N.check(lib.ls_gpu_block_gram(S, D, k, X.data_ptr(), Y.data_ptr(), G.data_ptr(), stream), "block Gram")
+        fn = lib.ls_gpu_block_gram_tc if _mode(X, dense) == "tensor" else lib.ls_gpu_block_gram
+        N.check(fn(S, D, k, X.data_ptr(), Y.data_ptr(), G.data_ptr(), stream), "block Gram")
         return G
     c = blocks
     while c > 1 and D // c < min_rows:

@@ -205,3 +205,89 @@ def test_sector_lanczos_tensor_equals_fp64():
     e_tc = lanczos.sector_ground_states(batch, steps=60, seed=2, graph=True, dense="tensor")
     e_fp64 = lanczos.sector_ground_states(batch, steps=60, seed=2, graph=True, dense="fp64")
     assert np.abs(e_tc - e_fp64).max() <= 1e-12 * np.abs(e_fp64).max()
+
+
+def gram_tc(X, Y):
+    import torch
+    S, D, k = X.shape
+    G = torch.empty((S, k, k), dtype=torch.complex128, device="cuda")
+    rc = N.lib().ls_gpu_block_gram_tc(S, D, k, X.data_ptr(), Y.data_ptr(), G.data_ptr(),
+                                      torch.cuda.current_stream().cuda_stream)
+    N.check(rc, "block Gram (tensor cores)")
+    torch.cuda.synchronize()
+    return G
+
+
+@pytest.mark.parametrize("S,D,k", [(1, 1, 1), (2, 129, 16), (3, 1000, 8), (1, 257, 5), (2, 300, 12),
+                                   (1, 128, 16), (3, 70001, 16), (5, 3000, 9)])
+def test_gram_tc_exact_on_small_integers(S, D, k):
+    import torch
+    X = int_block((S, D, k), 6, 1000)
+    Y = int_block((S, D, k), 7, 1000)
+    assert torch.equal(gram_tc(X, Y), X.mH @ Y)
+    assert torch.equal(gram_tc(X, X), X.mH @ X)
+
+
+def accurate_gram(A, B, rows=20000):
+    """X^H Y with every product rounded once and the sums over rows taken by tree reductions
+    (error ~ log2(D) u, where a GEMM's running sums give ~ sqrt(D) u)."""
+    import torch
+    S, D, k = A.shape
+    out = torch.zeros((S, k, k), dtype=torch.complex128, device="cuda")
+    for r0 in range(0, D, rows):
+        a, b = A[:, r0:r0 + rows], B[:, r0:r0 + rows]
+        out += (a.conj()[..., :, None] * b[..., None, :]).sum(dim=1)
+    return out
+
+
+@pytest.mark.parametrize("S,D,k,scale,spread", [
+    (1, 1000, 16, 1.0, 0.0), (3, 777, 8, 1e-6, 0.0), (2, 33, 3, 1e5, 0.0), (5, 4097, 16, 1.0, 3.0),
+    (2, 70001, 16, 1e-3, 0.0), (1, 200000, 5, 1.0, 1.0), (4, 31, 12, 1.0, 0.0),
+])
+def test_gram_tc_matches_fp64(S, D, k, scale, spread):
+    X = rand_block(S, D, k, seed=D + k, scale=scale, spread=spread)
+    Y = rand_block(S, D, k, seed=D + k + 1, scale=1.0 / scale, spread=spread)
+    for A, B in ((X, Y), (X, X)):
+        G = gram_tc(A, B)
+        ref = accurate_gram(A, B)
+        bound = A.abs().mT @ B.abs()
+        # FP64-level: 4e-15 of the sum of magnitudes (the FP32-pair kernel: 1e-13)
+        assert float(((G - ref).abs() / bound).max()) <= 4e-15
+
+
+def test_gram_tc_orthonormal_block_near_identity():
+    """The Gram of an orthonormal block: off-diagonal entries cancel to ~1e-16 (an absolute bound
+    that the FP32-pair kernel only meets to ~3e-14)."""
+    import torch
+    S, D, k = 3, 50000, 16
+    W = rand_block(S, D, k, seed=51)
+    Q = torch.linalg.qr(W)[0].contiguous()  # row-major [S, D, k], as the library expects
+    G = gram_tc(Q, Q)
+    eye = torch.eye(k, dtype=torch.complex128, device="cuda")
+    assert float((G - eye).abs().max()) < 5e-15
+
+
+def test_gram_tc_on_blocks_larger_than_l2_and_deterministic():
+    import torch
+    S, D, k = 4, 400000, 16
+    X = rand_block(S, D, k, seed=61)
+    Y = rand_block(S, D, k, seed=62)
+    G = gram_tc(X, Y)
+    ref = accurate_gram(X, Y)
+    assert float(((G - ref).abs() / (X.abs().mT @ Y.abs())).max()) <= 4e-15
+    assert torch.equal(G, gram_tc(X, Y))
+
+
+def test_gram_tc_empty_and_invalid():
+    import torch
+    X = torch.empty((3, 0, 4), dtype=torch.complex128, device="cuda")
+    G = torch.full((3, 4, 4), 7.0 + 1j, dtype=torch.complex128, device="cuda")
+    rc = N.lib().ls_gpu_block_gram_tc(3, 0, 4, X.data_ptr(), X.data_ptr(), G.data_ptr(),
+                                      torch.cuda.current_stream().cuda_stream)
+    N.check(rc, "block Gram (tensor cores)")
+    torch.cuda.synchronize()
+    assert float(G.abs().max()) == 0.0
+    Z = rand_block(1, 10, 17, seed=0)
+    rc = N.lib().ls_gpu_block_gram_tc(1, 10, 17, Z.data_ptr(), Z.data_ptr(), Z.data_ptr(), None)
+    assert rc == -1
+    assert "k <= 16" in N.lib().ls_gpu_last_error().decode()
