@@ -561,7 +561,8 @@ def run_hubbard(args):
                   "ground_state": {"E0": e0.item(), "lanczos_steps": c["lanczos_steps"], "seconds": t_lanczos,
                                    "dE0_dtheta_hellmann_feynman": hf, "dE0_dtheta_central_fd": fd,
                                    "fd_step": h, "theta": theta0,
-                                   "dense": "FP32-pair Gram / update kernels (ls_gpu_block_gram, ls_gpu_block_update)",
+                                   "dense": "tensor-core Gram / update kernels (ls_gpu_block_gram_tc, "
+                                            "ls_gpu_block_update_tc)",
                                    "E0_fp64_dense": e0_fp64, "seconds_fp64_dense": t_fp64}},
     }
     print(json.dumps(line))
@@ -709,19 +710,26 @@ def run_sectors(args):
     e2e = {"value": elements * k / te, "unit": "elements/s", "h2d_bytes_per_step": hx.numel() * 16,
            "d2h_bytes_per_step": hy.numel() * 16, "path": "SectorBatch.replay with pinned host X/Y copies"}
 
+    # dense products on the tensor cores (the default): the full recurrence and the lean one (one
+    # Cholesky-QR pass, no local re-orthogonalisation)
     timer = {}
-    e0 = lanczos.sector_ground_states(batch, steps=c["lanczos_steps"], seed=c["seed"], graph=True, timer=timer)
-    timer_lean = {}  # one Cholesky-QR pass, no local re-orthogonalisation
+    e0 = lanczos.sector_ground_states(batch, steps=c["lanczos_steps"], seed=c["seed"], graph=True, timer=timer,
+                                      dense="tensor")
+    timer_lean = {}
     e0_lean = lanczos.sector_ground_states(batch, steps=c["lanczos_steps"], seed=c["seed"], graph=True,
-                                           timer=timer_lean, lean=True)
-    # the same recurrence with torch FP64 GEMMs for the dense products (fewer steps on the large
-    # workload: FP64 GEMMs are slow on GB300)
+                                           timer=timer_lean, lean=True, dense="tensor")
+    # the same recurrence with the FP32-pair kernels and with torch FP64 GEMMs for the dense products
+    # (fewer steps on the large workload: FP64 GEMMs are slow on GB300)
     cmp_steps = c.get("lanczos_compare_steps", c["lanczos_steps"])
-    timer_pc = timer
-    e0_pc = e0
+    timer_tc = timer
+    e0_tc = e0
     if cmp_steps != c["lanczos_steps"]:
-        timer_pc = {}
-        e0_pc = lanczos.sector_ground_states(batch, steps=cmp_steps, seed=c["seed"], graph=True, timer=timer_pc)
+        timer_tc = {}
+        e0_tc = lanczos.sector_ground_states(batch, steps=cmp_steps, seed=c["seed"], graph=True, timer=timer_tc,
+                                             dense="tensor")
+    timer_pc = {}
+    e0_pc = lanczos.sector_ground_states(batch, steps=cmp_steps, seed=c["seed"], graph=True, timer=timer_pc,
+                                         dense="paired")
     timer_f = {}
     e0_f = lanczos.sector_ground_states(batch, steps=cmp_steps, seed=c["seed"], graph=True, timer=timer_f,
                                         dense="fp64")
@@ -774,15 +782,23 @@ def run_sectors(args):
                   "plain_one_vector_all_sectors_ms": t_plain,
                   "speedup_per_vector_vs_plain": t_plain * k / t_ms,
                   "lanczos": {"steps": c["lanczos_steps"], "ms_per_step": timer["ms"] / timer["steps"],
+                              "step_over_matvec": timer["ms"] / timer["steps"] / t_ms,
                               "ground_state_energy": float(np.min(e0)),
                               "sector_of_ground_state": int(np.argmin(e0)),
-                              "dense": "FP32-pair Gram / update kernels (ls_gpu_block_gram, ls_gpu_block_update)",
+                              "dense": "tensor-core Gram / update kernels (ls_gpu_block_gram_tc, "
+                                       "ls_gpu_block_update_tc: fixed-point bf16 digits, exact FP32 group "
+                                       "sums, FP64 results)",
                               "lean_ms_per_step": timer_lean["ms"] / timer_lean["steps"],
+                              "lean_step_over_matvec": timer_lean["ms"] / timer_lean["steps"] / t_ms,
                               "lean_max_abs_diff_sector_e0": float(np.max(np.abs(e0_lean - e0))),
-                              "fp64_dense": {"steps": cmp_steps, "ms_per_step": timer_f["ms"] / timer_f["steps"],
-                                             "paired_ms_per_step": timer_pc["ms"] / timer_pc["steps"],
-                                             "max_abs_diff_sector_e0_vs_paired":
-                                                 float(np.max(np.abs(e0_f - e0_pc)))}}},
+                              "compare": {"steps": cmp_steps,
+                                          "tensor_ms_per_step": timer_tc["ms"] / timer_tc["steps"],
+                                          "paired_ms_per_step": timer_pc["ms"] / timer_pc["steps"],
+                                          "fp64_ms_per_step": timer_f["ms"] / timer_f["steps"],
+                                          "max_abs_diff_sector_e0_tensor_vs_fp64":
+                                              float(np.max(np.abs(e0_tc - e0_f))),
+                                          "max_abs_diff_sector_e0_paired_vs_fp64":
+                                              float(np.max(np.abs(e0_pc - e0_f)))}}},
     }
     print(json.dumps(line))
     return 0

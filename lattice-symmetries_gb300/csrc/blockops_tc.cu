@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (it >= 1) {
       // the previous tile's MMAs are done (A and B free, its accumulators final) and every
       // thread has finished the epilogue before it (rowexp / colexp of this buffer free)
-      const bool ok = tc::mbar_wait(tc::smem_u32(&mbar[buf ^ 1]), ((it - 1) >> 1) & 1, kWaitCycles);
+      const bool ok = tid != 0 || tc::mbar_wait(tc::smem_u32(&mbar[buf ^ 1]), ((it - 1) >> 1) & 1, kWaitCycles);
       if (__syncthreads_or(!ok)) {
         failed = true;
         break;
@@ -351,13 +351,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc::fence_after_sync();
     if (tid == 0) {
 #pragma unroll
+      const uint64_t ad0 = tc::smem_desc(a0, Sh::a_kstride, kRowCore);
+      const uint64_t bd0 = tc::smem_desc(b0, Sh::b_kstride, kRowCore);
+      const uint32_t d0 = tmem + buf * (kDigits * Sh::NC);
+#pragma unroll
       for (int i = 0; i < kDigits; ++i) {
 #pragma unroll
         for (int ks = 0; ks < Sh::K / 16; ++ks) {
-          const uint64_t ad = tc::smem_desc(a0 + i * Sh::a_plane + ks * 2 * Sh::a_kstride, Sh::a_kstride, kRowCore);
-          const uint64_t bd = tc::smem_desc(b0 + ks * 2 * Sh::b_kstride, Sh::b_kstride, kRowCore);
-          tc::mma_bf16(tmem + buf * (kDigits * Sh::NC) + i * Sh::NC, ad, bd,
-                       tc::idesc_bf16_f32(kRows, Sh::NC * (kDigits - i)), (i > 0 || ks > 0) ? 1u : 0u);
+          // start addresses advance in the descriptors' low field (units of 16 bytes)
+          tc::mma_bf16(d0 + i * Sh::NC, ad0 + ((i * Sh::a_plane + ks * 2 * Sh::a_kstride) >> 4),
+                       bd0 + ((ks * 2 * Sh::b_kstride) >> 4), tc::idesc_bf16_f32(kRows, Sh::NC * (kDigits - i)),
+                       (i > 0 || ks > 0) ? 1u : 0u);
         }
       }
       tc::commit(tc::smem_u32(&mbar[buf]));
@@ -376,7 +380,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int n = (int)(t_end - t_begin);
   if (!failed && n >= 1) {
     const int lb = (n - 1) & 1;
-    const bool ok = tc::mbar_wait(tc::smem_u32(&mbar[lb]), ((n - 1) >> 1) & 1, kWaitCycles);
+    const bool ok = tid != 0 || tc::mbar_wait(tc::smem_u32(&mbar[lb]), ((n - 1) >> 1) & 1, kWaitCycles);
     if (__syncthreads_or(!ok)) {
       failed = true;
     } else {
@@ -643,7 +647,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int buf = it & 1;
     const int64_t s = tile / tiles_per_sector;
     if (it >= 1) {
-      const bool ok = tc::mbar_wait(tc::smem_u32(&mbar[buf ^ 1]), ((it - 1) >> 1) & 1, kWaitCycles);
+      const bool ok = tid != 0 || tc::mbar_wait(tc::smem_u32(&mbar[buf ^ 1]), ((it - 1) >> 1) & 1, kWaitCycles);
       if (__syncthreads_or(!ok)) {
         failed = true;
         break;
@@ -657,18 +661,20 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc::fence_after_sync();
     if (tid == 0) {
       const uint32_t d0 = tmem + buf * Sh::buf_cols;
-#pragma unroll 1
+      const uint64_t ad0 = tc::smem_desc(x0, Sh::x_kstride, kRowCore);
+      const uint64_t bd0 = tc::smem_desc(y0, yks, kRowCore);
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(kRows, Sh::NR);
+#pragma unroll
       for (int ks = 0; ks < kRows / 16; ++ks) {
 #pragma unroll
         for (int rho = 0; rho < Sh::REG; ++rho) {
-          const int jmax = min(kDigits - 1, rho * Sh::Q + Sh::Q - 1);
-          for (int j = 0; j <= jmax; ++j) {
+#pragma unroll
+          for (int j = 0; j <= (kDigits - 1 < rho * Sh::Q + Sh::Q - 1 ? kDigits - 1 : rho * Sh::Q + Sh::Q - 1); ++j) {
+            // start addresses advance in the descriptors' low field (units of 16 bytes)
             const uint32_t arow = (uint32_t)(Sh::Z + rho * Sh::Q - j) * Sh::NR;
-            const uint64_t ad =
-                tc::smem_desc(x0 + (arow / 8) * kRowCore + ks * 2 * Sh::x_kstride, Sh::x_kstride, kRowCore);
-            const uint64_t bd =
-                tc::smem_desc(y0 + (uint32_t)(j * Sh::NR / 8) * kRowCore + ks * 2 * yks, yks, kRowCore);
-            tc::mma_bf16(d0 + rho * Sh::NR, ad, bd, tc::idesc_bf16_f32(kRows, Sh::NR), (ks > 0 || j > 0) ? 1u : 0u);
+            tc::mma_bf16(d0 + rho * Sh::NR, ad0 + (((arow / 8) * kRowCore + ks * 2 * Sh::x_kstride) >> 4),
+                         bd0 + (((uint32_t)(j * Sh::NR / 8) * kRowCore + ks * 2 * yks) >> 4), idesc,
+                         (ks > 0 || j > 0) ? 1u : 0u);
           }
         }
       }
@@ -687,7 +693,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int n = (int)(t_end - t_begin);
   if (!failed && n >= 1) {
     const int lb = (n - 1) & 1;
-    const bool ok = tc::mbar_wait(tc::smem_u32(&mbar[lb]), ((n - 1) >> 1) & 1, kWaitCycles);
+    const bool ok = tid != 0 || tc::mbar_wait(tc::smem_u32(&mbar[lb]), ((n - 1) >> 1) & 1, kWaitCycles);
     if (__syncthreads_or(!ok)) {
       failed = true;
     } else {

@@ -17,10 +17,12 @@ and the eigenvalues of the block-tridiagonal T (diagonal blocks A_j, sub-diagona
 approximate the extremal eigenvalues of H.  There is no global re-orthogonalisation, so converged
 Ritz values can repeat ("ghosts"); the lowest ones are reliable.
 
-Dense products (`dense=`): "paired" (default on the GPU for k <= 16) runs the tall-skinny Gram
-matrices and block updates through the library's FP32-pair kernels (ls_gpu_block_gram /
-ls_gpu_block_update: FP64 storage, below 2^-45 relative error per product, several times the
-speed of FP64 GEMMs on GB300, whose FP64 pipe is narrow); "fp64" uses torch's FP64 GEMMs.
+Dense products (`dense=`): "tensor" (default on the GPU for k <= 16) runs the tall-skinny Gram
+matrices and block updates through the library's tensor-core kernels (ls_gpu_block_gram_tc /
+ls_gpu_block_update_tc: FP64 storage, values cut into fixed-point bf16 digits whose products are
+summed exactly by tcgen05 MMAs, FP64-level results); "paired" through its FP32-pair kernels
+(ls_gpu_block_gram / ls_gpu_block_update: below 2^-45 relative error per product); "fp64" uses
+torch's FP64 GEMMs (GB300's FP64 pipe is narrow: several times slower).
 CPU tensors always take the torch path.
 """
 
@@ -32,7 +34,7 @@ import numpy as np
 
 
 DENSE_MODES = ("tensor", "paired", "fp64")
-DENSE_DEFAULT = "paired"
+DENSE_DEFAULT = "tensor"
 
 
 def _mode(X, dense) -> str:
