@@ -255,15 +255,17 @@ __device__ __forceinline__ void update_epilogue(uint32_t tmem_buf, const int* ro
   for (int c = 0; c < KC; ++c)
     w[c] = (beta != 0.0 && live && j0 + c < k) ? W[(sec_base + row) * k + j0 + c] : make_double2(0.0, 0.0);
   long long H[RC];
-  uint32_t a[RC];
+  uint32_t a[kDigits][RC];
+  // all groups in flight at once, one wait
+#pragma unroll
+  for (int t = 0; t < kDigits; ++t) tc::tmem_ld<RC>(taddr + t * Sh::NC, a[t]);
+  tc::tmem_ld_wait();
   // groups 0 .. 6: Horner in base 2^7
 #pragma unroll
   for (int t = 0; t < kDigits; ++t) {
-    tc::tmem_ld<RC>(taddr + t * Sh::NC, a);
-    tc::tmem_ld_wait();
 #pragma unroll
     for (int c = 0; c < RC; ++c) {
-      const long long g = (long long)__float2int_rn(__uint_as_float(a[c]));
+      const long long g = (long long)__float2int_rn(__uint_as_float(a[t][c]));
       if (t == 0) H[c] = g;
       else if (t < kDigits - 1) H[c] = H[c] * 128 + g;
       else H[c] += g >> 7;  // group 7, truncated to the unit of group 6
@@ -443,22 +445,25 @@ int run_update_tc(int64_t S, int64_t D, int k, double beta, const double* d_w, c
 // column of X and of Y gets a frame over the tile's rows (its re and im parts share it, so that
 // the complex combination stays exact), and the digit planes are written transposed: element
 // (plane * NR + c, row) of a K-major operand, NR = 2 kp real columns.  One MMA with M = 128 covers
-// Q = 128 / NR consecutive planes of X; with the planes stacked in order behind Q - 1 zero planes,
-// lane block q of accumulator region rho collects exactly the products of weight t = rho Q + q:
-// for each plane j of Y, MMA(A = X planes rho Q - j .. rho Q - j + Q - 1, B = Y plane j) adds the
-// digit pairs (rho Q + q - j, j).  A cell sums at most 8 pairs x 128 rows of digit products,
-// |cell| <= 128 * 2^16 = 2^23 (exact in FP32).  After a tile the epilogue joins a lane's regions
-// into one 64-bit integer per column, converts it to FP64 with the tile's frames and adds it to
-// per-thread FP64 sums; at the end of a sector's rows the sums are reduced over lane blocks and
-// complex pairs into this CTA's partial Gram, and the partials are added over CTAs in a fixed
+// Q = 128 / NR consecutive planes a .. a + Q - 1 of X (lane block q = plane a + q; planes below 0
+// are zero planes stacked in front) and two planes j, j + 1 of Y (N = 2 NR).  Its first column
+// block then holds digit pairs of weight t = a + j + q, its second t = a + j + 1 + q.  With
+// MMAs (a = s - j, j) for s in {0, Q, ..} and even j, the two column blocks of region s are the
+// weights t = s + q (even j) and t = s + q + 1 (odd j) of lane block q, and every digit pair
+// (i, j) lands in exactly one cell.  A cell sums at most 4 pairs x 128 rows of digit products,
+// |cell| <= 2^23 (exact in FP32).  After a tile the epilogue joins a lane's cells into one 64-bit
+// integer per column (weights t = q .. q + 5 span 35 bits above a 2^23 cell: below 2^58),
+// converts it to FP64 with the tile's frames and adds it to per-thread FP64 sums; at the end of a
+// sector's rows the sums are reduced over lane blocks and complex pairs into this CTA's partial
+// Gram, and the partials are added over CTAs in a fixed
 // order by a second kernel (deterministic).
 
 template <int KP>
 struct GramShape {
-  static constexpr int NR = 2 * KP;      // real columns
-  static constexpr int Q = kRows / NR;   // digit planes per MMA: 4 (kp = 16) or 8 (kp = 8)
-  static constexpr int REG = kDigits / Q;  // accumulator regions: 2 or 1
-  static constexpr int Z = Q - 1;          // zero planes in front of X's planes
+  static constexpr int NR = 2 * KP;        // real columns
+  static constexpr int Q = kRows / NR;     // X digit planes per MMA: 4 (kp = 16) or 8 (kp = 8)
+  static constexpr int REG = kDigits / Q;  // accumulator regions (pairs of column blocks): 2 or 1
+  static constexpr int Z = Q == 4 ? 2 : 6; // zero planes in front of X's planes (lowest a = -Z)
   static constexpr int x_rows = (Z + kDigits) * NR;
   static constexpr int y_rows = kDigits * NR;
   static constexpr uint32_t x_kstride = x_rows * 16;
@@ -467,11 +472,12 @@ struct GramShape {
   static constexpr uint32_t y_bytes = (kRows / 8) * y_kstride;
   static constexpr uint32_t p_bytes = kRows * NR * 8;  // flush buffer: 128 lanes x NR doubles
   static constexpr uint32_t smem = x_bytes + y_bytes + p_bytes;
-  static constexpr uint32_t buf_cols = REG * NR;       // tensor-memory columns per tile
+  static constexpr uint32_t buf_cols = REG * 2 * NR;   // tensor-memory columns per tile
   static constexpr uint32_t tmem_cols = 2 * buf_cols < 32 ? 32 : 2 * buf_cols;
   static constexpr int units = NR * (kRows / 8);       // (column, 8-row group) units per operand
   static constexpr int PASSES = 2 * units / kThreads;  // units of X and Y per thread
   static constexpr int DC = NR / kParts;               // epilogue: columns of Y per thread
+  static constexpr int TOP = (REG - 1) * Q + 1;        // a lane's highest weight offset
 };
 
 template <int KP>
@@ -554,20 +560,27 @@ __device__ __forceinline__ void gram_epilogue(uint32_t tmem_buf, const int (*col
   const int l = quarter * 32 + lane;
   const int q = l / Sh::NR, c = l % Sh::NR;
   const uint32_t taddr = tmem_buf + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(part * Sh::DC);
-  uint32_t cell[Sh::REG][Sh::DC];
+  uint32_t cell[Sh::REG][2][Sh::DC];
 #pragma unroll
-  for (int rho = 0; rho < Sh::REG; ++rho) tc::tmem_ld<Sh::DC>(taddr + rho * Sh::NR, cell[rho]);
+  for (int r = 0; r < Sh::REG; ++r)
+#pragma unroll
+    for (int b = 0; b < 2; ++b) tc::tmem_ld<Sh::DC>(taddr + (r * 2 + b) * Sh::NR, cell[r][b]);
   tc::tmem_ld_wait();
   const int ec = colmax[0][c >> 1];
   const int* ey = colmax[same ? 0 : 1];
 #pragma unroll
   for (int dd = 0; dd < Sh::DC; ++dd) {
+    // weights t = r Q + b + q; unit = the weight of t = q + TOP
     long long v = 0;
 #pragma unroll
-    for (int rho = 0; rho < Sh::REG; ++rho) v = v * (1ll << (7 * Sh::Q)) + (long long)__float2int_rn(__uint_as_float(cell[rho][dd]));
+    for (int r = 0; r < Sh::REG; ++r) {
+      if (r > 0) v *= 1ll << (7 * (Sh::Q - 1));
+#pragma unroll
+      for (int b = 0; b < 2; ++b) v = v * (b == 0 ? 1ll : 128ll) + (long long)__float2int_rn(__uint_as_float(cell[r][b][dd]));
+    }
     const int ed = ey[(part * Sh::DC + dd) >> 1];
-    // v counts units of 2^(E_c + E_d - 14 - 7 q - 7 Q (REG - 1)), E = biased exponent - 1022
-    acc[dd] += int64_scaled_to_double(v, ec + ed - 2058 - 7 * q - 7 * Sh::Q * (Sh::REG - 1));
+    // v counts units of 2^(E_c + E_d - 14 - 7 (q + TOP)), E = biased exponent - 1022
+    acc[dd] += int64_scaled_to_double(v, ec + ed - 2058 - 7 * (q + Sh::TOP));
   }
 }
 
@@ -663,16 +676,18 @@ __global__ void __launch_bounds__(kThreads, 1)
       const uint32_t d0 = tmem + buf * Sh::buf_cols;
       const uint64_t ad0 = tc::smem_desc(x0, Sh::x_kstride, kRowCore);
       const uint64_t bd0 = tc::smem_desc(y0, yks, kRowCore);
-      constexpr uint32_t idesc = tc::idesc_bf16_f32(kRows, Sh::NR);
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(kRows, 2 * Sh::NR);
 #pragma unroll
       for (int ks = 0; ks < kRows / 16; ++ks) {
 #pragma unroll
-        for (int rho = 0; rho < Sh::REG; ++rho) {
+        for (int r = 0; r < Sh::REG; ++r) {
 #pragma unroll
-          for (int j = 0; j <= (kDigits - 1 < rho * Sh::Q + Sh::Q - 1 ? kDigits - 1 : rho * Sh::Q + Sh::Q - 1); ++j) {
+          for (int j = 0; j < kDigits; j += 2) {
+            const int a = r * Sh::Q - j;  // lowest X plane of this MMA
+            if (a + Sh::Q - 1 < 0) continue;  // only zero planes
             // start addresses advance in the descriptors' low field (units of 16 bytes)
-            const uint32_t arow = (uint32_t)(Sh::Z + rho * Sh::Q - j) * Sh::NR;
-            tc::mma_bf16(d0 + rho * Sh::NR, ad0 + (((arow / 8) * kRowCore + ks * 2 * Sh::x_kstride) >> 4),
+            const uint32_t arow = (uint32_t)(Sh::Z + a) * Sh::NR;
+            tc::mma_bf16(d0 + r * 2 * Sh::NR, ad0 + (((arow / 8) * kRowCore + ks * 2 * Sh::x_kstride) >> 4),
                          bd0 + (((uint32_t)(j * Sh::NR / 8) * kRowCore + ks * 2 * yks) >> 4), idesc,
                          (ks > 0 || j > 0) ? 1u : 0u);
           }
