@@ -265,7 +265,9 @@ __device__ __forceinline__ void update_epilogue(uint32_t tmem_buf, const int* ro
   for (int t = 0; t < kDigits; ++t) {
 #pragma unroll
     for (int c = 0; c < RC; ++c) {
-      const long long g = (long long)__float2int_rn(__uint_as_float(a[t][c]));
+      // |group sum| <= 2^22: adding 1.5 * 2^23 puts the integer in the low mantissa bits (FP32
+      // pipe, exact), instead of a float-to-integer conversion
+      const long long g = (long long)(__float_as_int(__fadd_rn(__uint_as_float(a[t][c]), 12582912.0f)) - 0x4b400000);
       if (t == 0) H[c] = g;
       else if (t < kDigits - 1) H[c] = H[c] * 128 + g;
       else H[c] += g >> 7;  // group 7, truncated to the unit of group 6
