@@ -28,13 +28,15 @@
 // product of length K over values of the frames' magnitudes.  Non-finite inputs are not
 // supported (the frame of a row or column holding inf or NaN is undefined).
 //
-// Work division: one persistent CTA of 256 threads per SM walks a contiguous range of 128-row
-// tiles (tiles never straddle sectors).  Per tile all 8 warps load the rows and write the bf16
-// digits of A (8 digit planes of 128 x K) into shared memory; one thread issues 8 MMAs per K
-// step (plane i against the digit planes j = 0..7-i of M at once, N = 2kp (8 - i), into the
-// accumulator columns of groups i..7) and commits them to an mbarrier; while those run, the
-// warps combine the previous tile from the other tensor-memory buffer (two buffers of 16 kp
-// columns).  M's digit image is built once per call by k_update_tc_prep.
+// Work division: one persistent CTA of 512 threads (16 warps) per SM walks a contiguous range of
+// 128-row tiles (tiles never straddle sectors).  Per tile all warps load the rows (one tile
+// ahead, in registers) and write the bf16 digits of A (8 digit planes of 128 x K) into shared
+// memory; one thread issues 8 MMAs per K step (plane i against the digit planes j = 0..7-i of M
+// at once, N = 2kp (8 - i), into the accumulator columns of groups i..7) and commits them to an
+// mbarrier; while those run, the warps combine the previous tile from the other tensor-memory
+// buffer (two buffers of 16 kp columns).  Only that thread polls the mbarrier; the others wait at
+// the CTA barrier.  M's digit image is built once per call by k_update_tc_prep.  The Gram kernel
+// below shares the digit code and the tile loop.
 #include "lsg.h"
 #include "tc.cuh"
 
@@ -457,8 +459,7 @@ int run_update_tc(int64_t S, int64_t D, int k, double beta, const double* d_w, c
 // integer per column (weights t = q .. q + 5 span 35 bits above a 2^23 cell: below 2^58),
 // converts it to FP64 with the tile's frames and adds it to per-thread FP64 sums; at the end of a
 // sector's rows the sums are reduced over lane blocks and complex pairs into this CTA's partial
-// Gram, and the partials are added over CTAs in a fixed
-// order by a second kernel (deterministic).
+// Gram, and the partials are added over CTAs in a fixed order by a second kernel (deterministic).
 
 template <int KP>
 struct GramShape {
