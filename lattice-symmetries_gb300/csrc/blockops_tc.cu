@@ -41,6 +41,9 @@
 #include "tc.cuh"
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <utility>
 
 namespace lsg {
 namespace {
@@ -70,6 +73,22 @@ struct UpdShape {
   static constexpr uint32_t tmem_cols = 2 * kDigits * NC;  // two accumulator buffers
   static constexpr uint32_t smem = a_bytes + b_bytes;
 };
+
+// Raises a kernel's dynamic shared-memory limit once per device (the attribute is per device).
+bool smem_attribute_set(const void* kern, uint32_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, uint32_t> done;
+  int dev = 0;
+  if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return false;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = done.find({kern, dev});
+  if (it != done.end() && it->second >= bytes) return true;
+  if (!cuda_ok(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes),
+               "cudaFuncSetAttribute(tensor-core block kernel)"))
+    return false;
+  done[{kern, dev}] = bytes;
+  return true;
+}
 
 // ---- digits ---------------------------------------------------------------------------------
 
@@ -356,7 +375,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     tc::fence_after_sync();
     if (tid == 0) {
-#pragma unroll
       const uint64_t ad0 = tc::smem_desc(a0, Sh::a_kstride, kRowCore);
       const uint64_t bd0 = tc::smem_desc(b0, Sh::b_kstride, kRowCore);
       const uint32_t d0 = tmem + buf * (kDigits * Sh::NC);
@@ -405,13 +423,7 @@ template <int KP>
 int run_update_tc(int64_t S, int64_t D, int k, double beta, const double* d_w, const double* d_x1,
                   const double* d_m1, const double* d_x2, const double* d_m2, double* d_out, cudaStream_t st) {
   using Sh = UpdShape<KP>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    if (!cuda_ok(cudaFuncSetAttribute(k_block_update_tc<KP>, cudaFuncAttributeMaxDynamicSharedMemorySize, Sh::smem),
-                 "cudaFuncSetAttribute(k_block_update_tc)"))
-      return LS_GPU_ERR_CUDA;
-    attr_set = true;
-  }
+  if (!smem_attribute_set((const void*)k_block_update_tc<KP>, Sh::smem)) return LS_GPU_ERR_CUDA;
   const int64_t tiles_per_sector = (D + kRows - 1) / kRows;
   const int64_t total = S * tiles_per_sector;
   const int grid = (int)std::min<int64_t>(total, (int64_t)num_sms());
@@ -729,13 +741,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 template <int KP>
 int run_gram_tc(int64_t S, int64_t D, int k, const double* d_x, const double* d_y, double* d_g, cudaStream_t st) {
   using Sh = GramShape<KP>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    if (!cuda_ok(cudaFuncSetAttribute(k_block_gram_tc<KP>, cudaFuncAttributeMaxDynamicSharedMemorySize, Sh::smem),
-                 "cudaFuncSetAttribute(k_block_gram_tc)"))
-      return LS_GPU_ERR_CUDA;
-    attr_set = true;
-  }
+  if (!smem_attribute_set((const void*)k_block_gram_tc<KP>, Sh::smem)) return LS_GPU_ERR_CUDA;
   const int64_t tiles_per_sector = (D + kRows - 1) / kRows;
   const int64_t total = S * tiles_per_sector;
   const int grid = (int)std::min<int64_t>(total, (int64_t)num_sms());
