@@ -193,43 +193,46 @@ __global__ void __launch_bounds__(kThreads) k_update_tc_prep(int k, const double
 
 // ---- the product kernel -----------------------------------------------------------------------
 
-template <int KP>
+// TWO: two terms (X1 M1 + X2 M2, K = 4 kp reals per row of A); one term uses the first 2 kp reals
+// only (half the digits and MMAs).
+template <int KP, bool TWO>
 struct UpdTile {
-  static constexpr int G = UpdShape<KP>::G;
-  static constexpr int RPW = 32 / G;               // rows per warp and pass
-  static constexpr int PASSES = kRows * G / kThreads;  // 2 (kp = 16) or 1 (kp = 8)
-  double2 v[PASSES][4];                            // this thread's 8 reals per pass
+  static constexpr int G = TWO ? UpdShape<KP>::G : UpdShape<KP>::G / 2;  // 8-real groups per row
+  static constexpr int RPW = 32 / G;                                      // rows per warp and pass
+  static constexpr int PASSES = (kRows * G + kThreads - 1) / kThreads;    // 2 or 1
+  double2 v[PASSES][4];                                                   // 8 reals per pass
 };
 
-template <int KP>
-__device__ __forceinline__ void update_load(UpdTile<KP>& t, int64_t tile_row0, int64_t D, int k, int64_t sec_base,
-                                            const double2* X1, const double2* X2) {
-  using T = UpdTile<KP>;
+template <int KP, bool TWO>
+__device__ __forceinline__ void update_load(UpdTile<KP, TWO>& t, int64_t tile_row0, int64_t D, int k,
+                                            int64_t sec_base, const double2* X1, const double2* X2) {
+  using T = UpdTile<KP, TWO>;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane % T::G;
-  const double2* X = g < T::G / 2 ? X1 : X2;
-  const int c0 = (g % (T::G / 2)) * 4;
+  const double2* X = (TWO && g >= T::G / 2) ? X2 : X1;
+  const int c0 = (TWO ? g % (T::G / 2) : g) * 4;
 #pragma unroll
   for (int p = 0; p < T::PASSES; ++p) {
     const int r = (p * kWarps + warp) * T::RPW + lane / T::G;
     const int64_t row = tile_row0 + r;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const bool in = row < D && c0 + q < k && X != nullptr;
+      const bool in = r < kRows && row < D && c0 + q < k;
       t.v[p][q] = in ? X[(sec_base + row) * k + c0 + q] : make_double2(0.0, 0.0);
     }
   }
 }
 
-template <int KP>
-__device__ __forceinline__ void update_produce(const UpdTile<KP>& t, uint8_t* A, int* rowexp) {
+template <int KP, bool TWO>
+__device__ __forceinline__ void update_produce(const UpdTile<KP, TWO>& t, uint8_t* A, int* rowexp) {
   using Sh = UpdShape<KP>;
-  using T = UpdTile<KP>;
+  using T = UpdTile<KP, TWO>;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane % T::G;
 #pragma unroll
   for (int p = 0; p < T::PASSES; ++p) {
     const int r = (p * kWarps + warp) * T::RPW + lane / T::G;
+    if ((p * kWarps + warp) * T::RPW >= kRows) break;  // this warp has no rows left (warp-uniform)
     int e = 0;
 #pragma unroll
     for (int q = 0; q < 4; ++q) e = max(e, max(exp_field(t.v[p][q].x), exp_field(t.v[p][q].y)));
@@ -311,7 +314,7 @@ __device__ __forceinline__ void update_epilogue(uint32_t tmem_buf, const int* ro
   }
 }
 
-template <int KP>
+template <int KP, bool TWO>
 __global__ void __launch_bounds__(kThreads, 1)
     k_block_update_tc(int64_t D, int k, int64_t tiles_per_sector, int64_t total_tiles, double beta,
                       const double2* W, const double2* X1, const double2* X2, const uint8_t* __restrict__ image,
@@ -343,10 +346,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   int64_t loaded_sector = -1;
   int64_t prev_row0 = 0, prev_base = 0;
   bool failed = false;
-  UpdTile<KP> regs;
+  UpdTile<KP, TWO> regs;
   if (t_begin < t_end) {
     const int64_t s = t_begin / tiles_per_sector;
-    update_load<KP>(regs, (t_begin % tiles_per_sector) * kRows, D, k, s * D, X1, X2);
+    update_load<KP, TWO>(regs, (t_begin % tiles_per_sector) * kRows, D, k, s * D, X1, X2);
   }
   for (int64_t tile = t_begin; tile < t_end; ++tile) {
     const int it = (int)(tile - t_begin);
@@ -369,7 +372,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       loaded_sector = s;
     }
     if (tid < Sh::NC) colexp[buf][tid] = col_exp[s * Sh::NC + tid];
-    update_produce<KP>(regs, A, rowexp[buf]);
+    update_produce<KP, TWO>(regs, A, rowexp[buf]);
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
@@ -381,7 +384,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
       for (int i = 0; i < kDigits; ++i) {
 #pragma unroll
-        for (int ks = 0; ks < Sh::K / 16; ++ks) {
+        for (int ks = 0; ks < (TWO ? Sh::K : Sh::K / 2) / 16; ++ks) {
           // start addresses advance in the descriptors' low field (units of 16 bytes)
           tc::mma_bf16(d0 + i * Sh::NC, ad0 + ((i * Sh::a_plane + ks * 2 * Sh::a_kstride) >> 4),
                        bd0 + ((ks * 2 * Sh::b_kstride) >> 4), tc::idesc_bf16_f32(kRows, Sh::NC * (kDigits - i)),
@@ -392,7 +395,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     if (tile + 1 < t_end) {
       const int64_t sn = (tile + 1) / tiles_per_sector;
-      update_load<KP>(regs, ((tile + 1) % tiles_per_sector) * kRows, D, k, sn * D, X1, X2);
+      update_load<KP, TWO>(regs, ((tile + 1) % tiles_per_sector) * kRows, D, k, sn * D, X1, X2);
     }
     if (it >= 1)
       update_epilogue<KP>(tmem + (buf ^ 1) * (kDigits * Sh::NC), rowexp[buf ^ 1], colexp[buf ^ 1], prev_row0, D, k,
@@ -423,7 +426,9 @@ template <int KP>
 int run_update_tc(int64_t S, int64_t D, int k, double beta, const double* d_w, const double* d_x1,
                   const double* d_m1, const double* d_x2, const double* d_m2, double* d_out, cudaStream_t st) {
   using Sh = UpdShape<KP>;
-  if (!smem_attribute_set((const void*)k_block_update_tc<KP>, Sh::smem)) return LS_GPU_ERR_CUDA;
+  const bool two = d_x2 != nullptr;
+  const void* kern = two ? (const void*)k_block_update_tc<KP, true> : (const void*)k_block_update_tc<KP, false>;
+  if (!smem_attribute_set(kern, Sh::smem)) return LS_GPU_ERR_CUDA;
   const int64_t tiles_per_sector = (D + kRows - 1) / kRows;
   const int64_t total = S * tiles_per_sector;
   const int grid = (int)std::min<int64_t>(total, (int64_t)num_sms());
@@ -443,10 +448,15 @@ int run_update_tc(int64_t S, int64_t D, int k, double beta, const double* d_w, c
     ok = cuda_ok(cudaGetLastError(), "k_update_tc_prep");
   }
   if (ok) {
-    k_block_update_tc<KP><<<grid, kThreads, Sh::smem, st>>>(
-        D, k, tiles_per_sector, total, beta, reinterpret_cast<const double2*>(d_w),
-        reinterpret_cast<const double2*>(d_x1), reinterpret_cast<const double2*>(d_x2), image, col_exp,
-        reinterpret_cast<double2*>(d_out), err);
+    if (two)
+      k_block_update_tc<KP, true><<<grid, kThreads, Sh::smem, st>>>(
+          D, k, tiles_per_sector, total, beta, reinterpret_cast<const double2*>(d_w),
+          reinterpret_cast<const double2*>(d_x1), reinterpret_cast<const double2*>(d_x2), image, col_exp,
+          reinterpret_cast<double2*>(d_out), err);
+    else
+      k_block_update_tc<KP, false><<<grid, kThreads, Sh::smem, st>>>(
+          D, k, tiles_per_sector, total, beta, reinterpret_cast<const double2*>(d_w),
+          reinterpret_cast<const double2*>(d_x1), nullptr, image, col_exp, reinterpret_cast<double2*>(d_out), err);
     ok = cuda_ok(cudaGetLastError(), "k_block_update_tc");
   }
   ok = cuda_ok(cudaFreeAsync(image, st), "cudaFreeAsync(update digits)") && ok;
