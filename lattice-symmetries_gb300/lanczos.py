@@ -49,7 +49,8 @@ def _mode(X, dense) -> str:
     return mode if native else "fp64"
 
 
-def _paired(X, dense) -> bool:
+def _library(X, dense) -> bool:
+    """True when the library's dense kernels (tensor-core or FP32-pair) take block X."""
     return _mode(X, dense) != "fp64"
 
 
@@ -69,7 +70,7 @@ def _gram(X, Y, dense=None, blocks: int = 256, min_rows: int = 64):
     import torch
 
     S, D, k = X.shape
-    if _paired(X, dense):
+    if _library(X, dense):
         N, lib = _native()
         X = X.contiguous()
         Y = Y.contiguous()
@@ -97,7 +98,7 @@ def _update(out, beta: float, W, X1, M1, X2=None, M2=None, dense=None):
     import torch
 
     S, D, k = X1.shape
-    if _paired(X1, dense) and out.is_contiguous():
+    if _library(X1, dense) and out.is_contiguous():
         N, lib = _native()
         X1 = X1.contiguous()
         M1 = M1.contiguous()
